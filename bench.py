@@ -1,0 +1,347 @@
+#!/usr/bin/env python
+"""Benchmark: forward + back projections per second at 128^3, interpFactor 2.
+
+Workload (one step): a seeded 128^3 Gaussian-blob volume (100 blobs) and
+10,000 directions on a 100 x 100 azimuth x cos-polar grid.  setVolume (CAS
+volume prepared on the device) -> forwardProject to 10,000 128^2 images ->
+reconstructVol of those images (back projection of the images, back
+projection of all-ones CAS images for the plane density, division, getVol).
+One step = 10,000 forward+back projection pairs.
+
+  value   device-resident inputs, timed with CUDA events on the stream the
+          library runs on (*_dev entry points), L2 flushed between steps.
+  e2e     the same step through the host-pointer C ABI with pinned host
+          buffers: volume and axes in, 10,000 images out, images back in,
+          volume out -- every host<->device copy inside the timed region.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "fwd+back projections/s at 128^3 x interp 2 (10,000 directions)"
+UNIT = "projection pairs/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="f32", choices=["f32", "f16", "bf16"])
+    ap.add_argument("--size", type=int, default=128)
+    ap.add_argument("--directions", type=int, default=10000)
+    ap.add_argument("--batch", type=int, default=2000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=64)
+    return ap.parse_args()
+
+
+def workload(args):
+    from oracle import oracle as O  # seeded synthetic inputs only (no checking here)
+
+    N = args.size
+    n_blobs = 100 if N == 128 else max(10, N // 2)
+    vol = O.blob_volume(N, n_blobs, seed=2)
+    side = int(round(args.directions ** 0.5))
+    if side * side == args.directions:
+        axes = O.grid_axes(side, side).astype(np.float32)
+    else:
+        axes = O.quaternion_axes(args.directions, seed=2).astype(np.float32)
+    return vol, axes
+
+
+def p_in(M, R):
+    c = M // 2
+    i = np.arange(M) - c
+    return int(np.sum((i[:, None] ** 2 + i[None, :] ** 2) <= R * R))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(vol, axes, args):
+    from oracle import cpu_path, oracle as O
+
+    p = O.Params(args.size)
+    S = min(args.cpu_sample, len(axes))
+    idx = np.linspace(0, len(axes) - 1, S).round().astype(int)
+    t_step, det = cpu_path.time_step(vol, axes[idx], p, len(axes))
+    return len(axes) / t_step, det, S
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    vol, axes = workload(args)
+    from oracle import cpu_path
+
+    vals = []
+    det = None
+    for s in range(args.warmup + args.steps):
+        v, det, S = cpu_baseline(vol, axes, args)
+        if s >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    cores = det["threads"]
+    sample = ("%d of the %d directions (evenly spaced) through the restated reference path: FP32 CAS prep "
+              "(scipy.fft), forward-projection kernel, 2-D FFTs, back projection and plane density "
+              "(gg_oracle.c, OpenMP), getVol; step time extrapolated as t_fixed + D/S * t_sample"
+              % (S, len(axes)))
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": len(axes) / value * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded Gaussian-blob volume, 100x100 direction grid)",
+           "config": {"workload": "128^3 volume, interpFactor 2 (CAS volume 262^3), 10,000 directions, "
+                                  "forwardProject + reconstructVol", "N": args.size, "directions": len(axes)},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "details": det}
+    print(json.dumps(out), flush=True)
+
+
+def run_gb300(args):
+    import torch
+    import torch.distributed as dist
+
+    import multigpugridder_gb300 as gg
+    from multigpugridder_gb300._lib import (GG_KERNEL_BACK, GG_KERNEL_DENSITY, GG_KERNEL_FORWARD, check, lib)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = lib()
+
+    vol, axes = workload(args)
+    n = len(axes)
+    N = args.size
+    g = gg.MultiGPUGridder(N, n, 2.0, GPUs=[local], MaxAxesToAllocate=args.batch, precision=args.precision)
+    h = g.handle
+    M, V, R = g.M, g.V, int(g.MaskRadius)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    d_vol = torch.from_numpy(vol).to(dev)
+    d_axes = torch.from_numpy(axes).to(dev)
+    d_imgs = torch.empty((n, N, N), dtype=torch.float32, device=dev)
+    d_out = torch.empty((N, N, N), dtype=torch.float32, device=dev)
+    l2 = torch.cuda.get_device_properties(dev).L2_cache_size if hasattr(torch.cuda.get_device_properties(dev), "L2_cache_size") else 128 << 20
+    flush = torch.empty(max(4 * l2, 512 << 20) // 4, dtype=torch.float32, device=dev)
+
+    def vp(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    def step():
+        check(L.gg_set_volume_dev(h, vp(d_vol), sp), h)
+        check(L.gg_forward_project_dev(h, vp(d_axes), n, vp(d_imgs), None, sp), h)
+        check(L.gg_reconstruct_volume_dev(h, vp(d_axes), n, vp(d_imgs), vp(d_out), sp), h)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+            flush.fill_(1.0)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    check(L.gg_profile_enable(h, 1), h)
+    launches0 = L.gg_kernel_launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+            flush.fill_(float(k))  # untimed L2 flush between steps
+    torch.cuda.synchronize()
+    launches = L.gg_kernel_launch_count() - launches0
+    ms_steps = [a.elapsed_time(b) for a, b in ev]
+    prof = {}
+    for name, kid in (("forward", GG_KERNEL_FORWARD), ("back", GG_KERNEL_BACK), ("density", GG_KERNEL_DENSITY)):
+        tot = ctypes.c_double()
+        cnt = ctypes.c_longlong()
+        check(L.gg_profile_read(h, kid, ctypes.byref(tot), ctypes.byref(cnt)), h)
+        prof[name] = (tot.value, cnt.value)
+    check(L.gg_profile_enable(h, 0), h)
+    clk = clocks.stop()
+    ms = sum(ms_steps)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * n / (ms_per_step / 1e3)
+
+    # roofline of the dominant kernel: algorithmic bytes per unit (one image)
+    #   forward  4*P_in*125 + 4*M^2   (taps gathered + CAS image written)
+    #   back     4*P_in*125 + s*M^2   (taps accumulated + CAS image read)
+    #   density  4*P_in*125           (all-ones images are not read)
+    s = 4 if args.precision == "f32" else 2
+    pin = p_in(M, R)
+    bpu = {"forward": s * pin * 125 + 4 * M * M, "back": 4 * pin * 125 + s * M * M, "density": 4 * pin * 125}
+    dom = max(prof, key=lambda k: prof[k][0])
+    tot_ms, cnt = prof[dom]
+    units_per_launch = n * args.steps / max(cnt, 1)
+    achieved = bpu[dom] * units_per_launch / (tot_ms / max(cnt, 1) / 1e3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs") or 6800.0
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": "measured" if peaks.get("hbm_gbs") else "fallback",
+                "traffic": None, "bytes_per_unit": bpu[dom], "units_per_launch": units_per_launch,
+                "kernel_ms": {k: v[0] / args.steps for k, v in prof.items()}}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, g, vol, axes, world)
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, det, S = cpu_baseline(vol, axes, args)
+        base = {"value": v, "unit": UNIT, "cores": det["threads"], "kind": "port",
+                "sample": "%d of %d directions timed, step extrapolated (t_fixed + D/S * t_sample)" % (S, n)}
+
+    g.close()
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": args.precision,
+               "data": "synthetic (seeded Gaussian-blob volume, 100x100 direction grid)",
+               "config": {"workload": "128^3 volume, interpFactor 2 (CAS volume 262^3, CAS images 256^2), "
+                                      "10,000 directions: setVolume + forwardProject + reconstructVol",
+                          "N": N, "M": M, "V": V, "directions": n, "batch": args.batch,
+                          "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
+                          "l2": "inputs larger than L2 (10,000 images = %d MB per step) and an untimed %d MB "
+                                "write between steps" % (n * N * N * 4 >> 20, flush.numel() * 4 >> 20)},
+               "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
+               "clocks": clk, "step_ms": ms_steps}
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_e2e(args, g, vol, axes, world):
+    """The same step through the host-pointer ABI with pinned host buffers."""
+    import torch
+
+    from multigpugridder_gb300._lib import check, lib
+
+    L = lib()
+    h = g.handle
+    n, N = len(axes), args.size
+    h_vol = torch.from_numpy(vol).pin_memory()
+    h_axes = torch.from_numpy(axes).pin_memory()
+    h_imgs = torch.empty((n, N, N), dtype=torch.float32).pin_memory()
+    h_out = torch.empty((N, N, N), dtype=torch.float32).pin_memory()
+    dims = (ctypes.c_int * 3)(N, N, N)
+
+    def vp(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    def step():
+        check(L.gg_set_volume(h, vp(h_vol), dims), h)
+        check(L.gg_forward_project(h, vp(h_axes), n, vp(h_imgs), None), h)
+        check(L.gg_reconstruct_volume(h, vp(h_axes), n, vp(h_imgs), vp(h_out)), h)
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.steps
+    ok = bool(np.isfinite(h_out.numpy()).all())
+    h2d = vol.nbytes + 2 * axes.nbytes + n * N * N * 4
+    d2h = n * N * N * 4 + vol.nbytes
+    return {"value": world * n / dt, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "ms_per_step": dt * 1e3, "finite": ok}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,580 @@
+// CAS ("cosine and sine") conversions around the FFTs, for GB300 (sm_103a).
+//
+// The reference chains separate element-wise kernels around cuFFT C2C calls
+// (pad, real->complex, fftshift, FFT, fftshift, complex->CAS, ...;
+// src/Gridders/gpuGridder.cpp:432-596, src/Matlab/utils/CASFromVol_Gridder.m,
+// volFromCAS_Gridder.m).  Here each chain is one pre-kernel and one
+// post-kernel around a real-to-complex or complex-to-real cuFFT transform:
+//   * the fftshifts (even sizes) become index remaps, folded into the loads
+//     and stores of the neighbouring kernel;
+//   * FromCAS yields an exactly Hermitian spectrum (c[-k] = conj(c[k]), the
+//     Nyquist row/column/slice zeroed), so the inverse transform is C2R and
+//     "take the real part" is free;
+//   * a real input makes the forward transform R2C; the other half of the
+//     spectrum is read through conjugate symmetry when forming Re+Im.
+#include <stdint.h>
+
+#include "gg_common.cuh"
+#include "gg_internal.h"
+#include "../../include/gg_gridder.h"
+
+namespace gg {
+
+static inline unsigned grid_for(size_t count, int threads)
+{
+    size_t g = (count + threads - 1) / threads;
+    if (g > 0x7fffffffull) g = 0x7fffffffull;
+    return (unsigned)(g ? g : 1);
+}
+
+__device__ __forceinline__ int shift_idx(int q, int M) { return q + M / 2 >= M ? q + M / 2 - M : q + M / 2; }
+
+// ---- 3-D: volume -> CAS volume --------------------------------------------
+
+// x[q] = (zero-padded volume * precomp^3)[(q + M/2) mod M] per axis.
+__global__ void vol_to_fft_input_kernel(const float *__restrict__ vol, int N, int M,
+                                        const double *__restrict__ pc, float *__restrict__ x)
+{
+    const size_t total = (size_t)M * M * M;
+    const int b = M / 2 - N / 2;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int qi = (int)(e % M), qj = (int)((e / M) % M), qk = (int)(e / ((size_t)M * M));
+        const int i = shift_idx(qi, M), j = shift_idx(qj, M), k = shift_idx(qk, M);
+        const int oi = i - b, oj = j - b, ok = k - b;
+        float v = 0.0f;
+        if ((unsigned)oi < (unsigned)N && (unsigned)oj < (unsigned)N && (unsigned)ok < (unsigned)N) {
+            const float f = (float)(pc[i] * pc[j] * pc[k]);
+            v = vol[(size_t)ok * N * N + (size_t)oj * N + oi] * f;
+        }
+        x[e] = v;
+    }
+}
+
+// CAS[pad+k][pad+j][pad+i] = Re+Im of fftshift(Y)[k][j][i]; border zero.
+template <typename T>
+__global__ void spectrum_to_cas_volume_kernel(const cufftComplex *__restrict__ spec, int M, int V, T *__restrict__ cas,
+                                              const float *__restrict__ d_scale)
+{
+    const float inv_scale = d_scale ? 1.0f / *d_scale : 1.0f;
+    const size_t total = (size_t)V * V * V;
+    const int pad = V / 2 - M / 2;
+    const int H = M / 2 + 1;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int ci = (int)(e % V), cj = (int)((e / V) % V), ck = (int)(e / ((size_t)V * V));
+        const int i = ci - pad, j = cj - pad, k = ck - pad;
+        float out = 0.0f;
+        if ((unsigned)i < (unsigned)M && (unsigned)j < (unsigned)M && (unsigned)k < (unsigned)M) {
+            const int u = shift_idx(i, M), v = shift_idx(j, M), w = shift_idx(k, M);
+            if (u <= M / 2) {
+                const cufftComplex c = spec[((size_t)w * M + v) * H + u];
+                out = c.x + c.y;
+            } else {  // conjugate symmetry: Y[w][v][u] = conj(Y[-w][-v][-u])
+                const int w2 = w ? M - w : 0, v2 = v ? M - v : 0, u2 = M - u;
+                const cufftComplex c = spec[((size_t)w2 * M + v2) * H + u2];
+                out = c.x - c.y;
+            }
+        }
+        cas[e] = from_f32<T>(out * inv_scale);
+    }
+}
+
+// ---- 3-D: CAS volume -> volume ---------------------------------------------
+
+// H[w][v][u] = FromCAS(crop(cas))[(w+M/2)%M][(v+M/2)%M][(u+M/2)%M], u <= M/2.
+__global__ void cas_volume_to_spectrum_kernel(const float *__restrict__ cas, int V, int M, cufftComplex *__restrict__ spec)
+{
+    const int H = M / 2 + 1;
+    const size_t total = (size_t)M * M * H;
+    const int b = V / 2 - M / 2;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int u = (int)(e % H), v = (int)((e / H) % M), w = (int)(e / ((size_t)H * M));
+        const int i = shift_idx(u, M), j = shift_idx(v, M), k = shift_idx(w, M);
+        cufftComplex c;
+        c.x = 0.0f;
+        c.y = 0.0f;
+        if (i != 0 && j != 0 && k != 0) {
+            const float r1 = cas[((size_t)(k + b) * V + (j + b)) * V + (i + b)];
+            const float r2 = cas[((size_t)(M - k + b) * V + (M - j + b)) * V + (M - i + b)];
+            c.x = 0.5f * (r1 + r2);
+            c.y = 0.5f * (r1 - r2);
+        }
+        spec[e] = c;
+    }
+}
+
+// vol[k][j][i] = y[(k+ob+M/2)%M]... / M^3 * precomp, centred crop.
+__global__ void fft_output_to_vol_kernel(const float *__restrict__ y, int M, int N, const double *__restrict__ pc,
+                                         float *__restrict__ vol)
+{
+    const size_t total = (size_t)N * N * N;
+    const int ob = M / 2 - N / 2;
+    const double inv = 1.0 / ((double)M * M * M);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int oi = (int)(e % N), oj = (int)((e / N) % N), ok = (int)(e / ((size_t)N * N));
+        const int i = oi + ob, j = oj + ob, k = ok + ob;
+        const float val = y[((size_t)shift_idx(k, M) * M + shift_idx(j, M)) * M + shift_idx(i, M)];
+        vol[e] = (float)((double)val * inv * pc[i] * pc[j] * pc[k]);
+    }
+}
+
+// ---- 2-D: CAS images -> images (forward-projection output path) -----------
+
+__global__ void cas_images_to_spectrum_kernel(const float *__restrict__ cas, int M, int n, cufftComplex *__restrict__ spec)
+{
+    const int H = M / 2 + 1;
+    const size_t per = (size_t)M * H;
+    const size_t total = per * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t a = e / per;
+        const int rem = (int)(e - a * per);
+        const int u = rem % H, v = rem / H;
+        const int i = shift_idx(u, M), j = shift_idx(v, M);
+        cufftComplex c;
+        c.x = 0.0f;
+        c.y = 0.0f;
+        if (i != 0 && j != 0) {
+            const float *img = cas + a * M * M;
+            const float r1 = img[(size_t)j * M + i];
+            const float r2 = img[(size_t)(M - j) * M + (M - i)];
+            c.x = 0.5f * (r1 + r2);
+            c.y = 0.5f * (r1 - r2);
+        }
+        spec[e] = c;
+    }
+}
+
+__global__ void fft_output_to_images_kernel(const float *__restrict__ y, int M, int N, int n, float *__restrict__ img)
+{
+    const size_t per = (size_t)N * N;
+    const size_t total = per * n;
+    const int ob = (M - N) / 2;
+    const float scale = 1.0f / ((float)M * (float)M);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t a = e / per;
+        const int rem = (int)(e - a * per);
+        const int oi = rem % N, oj = rem / N;
+        const int i = shift_idx(oi + ob, M), j = shift_idx(oj + ob, M);
+        img[e] = y[a * M * M + (size_t)j * M + i] * scale;
+    }
+}
+
+// ---- 2-D: images -> CAS images (back-projection input path) --------------
+
+__global__ void images_to_fft_input_kernel(const float *__restrict__ img, int N, int M, int n, float *__restrict__ x)
+{
+    const size_t per = (size_t)M * M;
+    const size_t total = per * n;
+    const int b = (M - N) / 2;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t a = e / per;
+        const int rem = (int)(e - a * per);
+        const int qi = rem % M, qj = rem / M;
+        const int oi = shift_idx(qi, M) - b, oj = shift_idx(qj, M) - b;
+        float v = 0.0f;
+        if ((unsigned)oi < (unsigned)N && (unsigned)oj < (unsigned)N) v = img[a * N * N + (size_t)oj * N + oi];
+        x[e] = v;
+    }
+}
+
+template <typename T>
+__global__ void spectrum_to_cas_images_kernel(const cufftComplex *__restrict__ spec, int M, int n, T *__restrict__ cas,
+                                              const float *__restrict__ d_scale)
+{
+    const float inv_scale = d_scale ? 1.0f / *d_scale : 1.0f;
+    const int H = M / 2 + 1;
+    const size_t per = (size_t)M * M;
+    const size_t total = per * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t a = e / per;
+        const int rem = (int)(e - a * per);
+        const int i = rem % M, j = rem / M;
+        const int u = shift_idx(i, M), v = shift_idx(j, M);
+        const cufftComplex *s = spec + a * (size_t)M * H;
+        float out;
+        if (u <= M / 2) {
+            const cufftComplex c = s[(size_t)v * H + u];
+            out = c.x + c.y;
+        } else {
+            const int v2 = v ? M - v : 0;
+            const cufftComplex c = s[(size_t)v2 * H + (M - u)];
+            out = c.x - c.y;
+        }
+        cas[e] = from_f32<T>(out * inv_scale);
+    }
+}
+
+__global__ void divide_plane_density_kernel(float *__restrict__ a, const float *__restrict__ b, size_t count, float eps)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        a[e] = a[e] / (b[e] + eps);
+}
+
+template <typename T>
+__global__ void convert_kernel(const float *__restrict__ in, T *__restrict__ out, size_t count, const float *__restrict__ d_scale)
+{
+    const float inv_scale = d_scale ? 1.0f / *d_scale : 1.0f;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        out[e] = from_f32<T>(in[e] * inv_scale);
+}
+
+// Non-negative floats order like their bit patterns, so an unsigned atomicMax
+// on the bits of |x| finds the largest magnitude.
+__global__ void max_abs_kernel(const float *__restrict__ x, size_t count, unsigned int *out)
+{
+    float m = 0.0f;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(x[e]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+__global__ void scale_from_max_kernel(unsigned int *work, float target, float *d_scale)
+{
+    const float m = __uint_as_float(*work);
+    float sc = 1.0f;
+    while (sc < 1e30f && m / sc > target) sc *= 2.0f;
+    *d_scale = sc;
+    *work = 0u;  // ready for the next use
+}
+
+// ---- launchers -------------------------------------------------------------
+
+constexpr int kT = 256;
+
+cudaError_t launch_vol_to_fft_input(const float *d_vol, int N, int M, const double *d_precomp, float *d_x, cudaStream_t s)
+{
+    vol_to_fft_input_kernel<<<grid_for((size_t)M * M * M, kT), kT, 0, s>>>(d_vol, N, M, d_precomp, d_x);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectrum_to_cas_volume(const cufftComplex *d_spec, int M, int V, void *d_cas, int prec,
+                                          const float *d_scale, cudaStream_t s)
+{
+    const unsigned g = grid_for((size_t)V * V * V, kT);
+    if (prec == kF32) spectrum_to_cas_volume_kernel<float><<<g, kT, 0, s>>>(d_spec, M, V, (float *)d_cas, d_scale);
+    else if (prec == kF16) spectrum_to_cas_volume_kernel<__half><<<g, kT, 0, s>>>(d_spec, M, V, (__half *)d_cas, d_scale);
+    else spectrum_to_cas_volume_kernel<__nv_bfloat16><<<g, kT, 0, s>>>(d_spec, M, V, (__nv_bfloat16 *)d_cas, d_scale);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cas_volume_to_spectrum(const float *d_cas, int V, int M, cufftComplex *d_spec, cudaStream_t s)
+{
+    cas_volume_to_spectrum_kernel<<<grid_for((size_t)M * M * (M / 2 + 1), kT), kT, 0, s>>>(d_cas, V, M, d_spec);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fft_output_to_vol(const float *d_y, int M, int N, const double *d_precomp, float *d_vol, cudaStream_t s)
+{
+    fft_output_to_vol_kernel<<<grid_for((size_t)N * N * N, kT), kT, 0, s>>>(d_y, M, N, d_precomp, d_vol);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cas_images_to_spectrum(const float *d_cas, int M, int n, cufftComplex *d_spec, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    cas_images_to_spectrum_kernel<<<grid_for((size_t)M * (M / 2 + 1) * n, kT), kT, 0, s>>>(d_cas, M, n, d_spec);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fft_output_to_images(const float *d_y, int M, int N, int n, float *d_img, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    fft_output_to_images_kernel<<<grid_for((size_t)N * N * n, kT), kT, 0, s>>>(d_y, M, N, n, d_img);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_images_to_fft_input(const float *d_img, int N, int M, int n, float *d_x, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    images_to_fft_input_kernel<<<grid_for((size_t)M * M * n, kT), kT, 0, s>>>(d_img, N, M, n, d_x);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectrum_to_cas_images(const cufftComplex *d_spec, int M, int n, void *d_cas, int prec,
+                                          const float *d_scale, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const unsigned g = grid_for((size_t)M * M * n, kT);
+    if (prec == kF32) spectrum_to_cas_images_kernel<float><<<g, kT, 0, s>>>(d_spec, M, n, (float *)d_cas, d_scale);
+    else if (prec == kF16) spectrum_to_cas_images_kernel<__half><<<g, kT, 0, s>>>(d_spec, M, n, (__half *)d_cas, d_scale);
+    else spectrum_to_cas_images_kernel<__nv_bfloat16><<<g, kT, 0, s>>>(d_spec, M, n, (__nv_bfloat16 *)d_cas, d_scale);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_divide_plane_density(float *d_a, const float *d_b, size_t count, float eps, cudaStream_t s)
+{
+    divide_plane_density_kernel<<<grid_for(count, kT), kT, 0, s>>>(d_a, d_b, count, eps);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_convert(const float *d_in, void *d_out, int prec, size_t count, const float *d_scale, cudaStream_t s)
+{
+    const unsigned g = grid_for(count, kT);
+    if (prec == kF32) convert_kernel<float><<<g, kT, 0, s>>>(d_in, (float *)d_out, count, d_scale);
+    else if (prec == kF16) convert_kernel<__half><<<g, kT, 0, s>>>(d_in, (__half *)d_out, count, d_scale);
+    else convert_kernel<__nv_bfloat16><<<g, kT, 0, s>>>(d_in, (__nv_bfloat16 *)d_out, count, d_scale);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_storage_scale(const float *d_x, size_t count, float target, unsigned int *d_work, float *d_scale,
+                                 cudaStream_t s)
+{
+    // d_work is left at zero by the previous use (and by the allocator's memset)
+    unsigned g = grid_for(count, kT);
+    if (g > 4096) g = 4096;
+    max_abs_kernel<<<g, kT, 0, s>>>(d_x, count, d_work);
+    scale_from_max_kernel<<<1, 1, 0, s>>>(d_work, target, d_scale);
+    count_launches(2);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// The reference's filters (src/Filters/*.cu) as building blocks.
+// Slices are size x size; n_slices = 0 means a size^3 volume.
+// ---------------------------------------------------------------------------
+
+__global__ void f_complex_to_cas(const float2 *__restrict__ c, float *__restrict__ r, size_t count)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        r[e] = c[e].x + c[e].y;
+}
+
+__global__ void f_cas_to_complex(const float *__restrict__ r, float2 *__restrict__ c, int size, int nsl, bool vol3)
+{
+    const size_t per = (size_t)size * size;
+    const size_t count = per * nsl;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % size), j = (int)((e / size) % size), k = (int)(e / per);
+        float2 out = make_float2(0.f, 0.f);
+        if (i != 0 && j != 0 && (!vol3 || k != 0)) {
+            const int k2 = vol3 ? size - k : k;
+            const float a = r[e], b = r[(size_t)k2 * per + (size_t)(size - j) * size + (size - i)];
+            out = make_float2(0.5f * (a + b), 0.5f * (a - b));
+        }
+        c[e] = out;
+    }
+}
+
+template <typename T>
+__global__ void f_fftshift_2d(T *d, int size, int nsl)
+{
+    // swap quadrant pairs: each thread owns one element of the top half
+    const int h = size / 2;
+    const size_t per_half = (size_t)size * h;
+    const size_t count = per_half * nsl;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = e / per_half;
+        const int rem = (int)(e - s * per_half);
+        const int i = rem % size, j = rem / size;  // j < h
+        T *img = d + s * size * size;
+        const size_t p = (size_t)j * size + i;
+        const size_t q = (size_t)(j + h) * size + (i + h) % size;
+        T tmp = img[p];
+        img[p] = img[q];
+        img[q] = tmp;
+    }
+}
+
+template <typename T>
+__global__ void f_fftshift_3d(T *d, int size)
+{
+    const int h = size / 2;
+    const size_t per = (size_t)size * size;
+    const size_t count = per * h;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % size), j = (int)((e / size) % size), k = (int)(e / per);  // k < h
+        const size_t p = (size_t)k * per + (size_t)j * size + i;
+        const size_t q = (size_t)(k + h) * per + (size_t)((j + h) % size) * size + (i + h) % size;
+        T tmp = d[p];
+        d[p] = d[q];
+        d[q] = tmp;
+    }
+}
+
+__global__ void f_pad(const float *__restrict__ in, float *__restrict__ out, int ix, int iy, int iz, int px, int py, int pz)
+{
+    const int ox = ix + 2 * px, oy = iy + 2 * py, oz = iz + 2 * pz;
+    const size_t count = (size_t)ox * oy * oz;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % ox) - px, j = (int)((e / ox) % oy) - py, k = (int)(e / ((size_t)ox * oy)) - pz;
+        float v = 0.f;
+        if ((unsigned)i < (unsigned)ix && (unsigned)j < (unsigned)iy && (unsigned)k < (unsigned)iz)
+            v = in[((size_t)k * iy + j) * ix + i];
+        out[e] = v;
+    }
+}
+
+__global__ void f_crop(const float *__restrict__ in, float *__restrict__ out, int ix, int iy, int iz, int cx, int cy, int cz)
+{
+    const int ox = ix - 2 * cx, oy = iy - 2 * cy, oz = iz - 2 * cz;
+    const size_t count = (size_t)ox * oy * oz;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(e % ox), j = (int)((e / ox) % oy), k = (int)(e / ((size_t)ox * oy));
+        out[e] = in[((size_t)(k + cz) * iy + (j + cy)) * ix + (i + cx)];
+    }
+}
+
+__global__ void f_divide_volumes(float *a, const float *__restrict__ b, size_t count)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        a[e] = (a[e] != 0.f && b[e] != 0.f) ? a[e] / b[e] : 0.f;
+}
+
+__global__ void f_multiply(float *a, const float *__restrict__ b, size_t count, bool a_complex)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x) {
+        if (a_complex) {
+            a[2 * e] *= b[e];
+            a[2 * e + 1] *= b[e];
+        } else {
+            a[e] *= b[e];
+        }
+    }
+}
+
+__global__ void f_add(float *a, const float *__restrict__ b, size_t count)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        a[e] += b[e];
+}
+
+__global__ void f_div_scalar(float *a, float s, size_t count)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        a[e] = a[e] / s;
+}
+
+__global__ void f_real_to_complex(const float *__restrict__ r, float2 *__restrict__ c, size_t count)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        c[e] = make_float2(r[e], 0.f);
+}
+
+__global__ void f_complex_to_real(const float2 *__restrict__ c, float *__restrict__ r, size_t count)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        r[e] = c[e].x;
+}
+
+} // namespace gg
+
+using namespace gg;
+
+static size_t slice_count(int size, int n_slices) { return (size_t)size * size * (size_t)(n_slices > 0 ? n_slices : size); }
+
+#define GG_FILTER_RET()                                                \
+    count_launches(1);                                                 \
+    return cudaGetLastError() == cudaSuccess ? GG_OK : GG_ERR_CUDA
+
+extern "C" int gg_filter_complex_to_cas(const float *d_complex, float *d_cas, int size, int n_slices, void *stream)
+{
+    if (size <= 0 || n_slices < 0 || !d_complex || !d_cas) return GG_ERR_INVALID_ARG;
+    const size_t c = slice_count(size, n_slices);
+    f_complex_to_cas<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>((const float2 *)d_complex, d_cas, c);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_cas_to_complex(const float *d_cas, float *d_complex, int size, int n_slices, void *stream)
+{
+    if (size <= 0 || n_slices < 0 || !d_complex || !d_cas) return GG_ERR_INVALID_ARG;
+    const bool vol3 = n_slices == 0;
+    const int nsl = vol3 ? size : n_slices;
+    f_cas_to_complex<<<grid_for(slice_count(size, nsl), kT), kT, 0, (cudaStream_t)stream>>>(d_cas, (float2 *)d_complex, size, nsl, vol3);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_fftshift_2d(float *d_data, int complex_elems, int size, int n_slices, void *stream)
+{
+    if (size <= 0 || (size & 1) || n_slices <= 0 || !d_data) return GG_ERR_INVALID_ARG;
+    const unsigned g = grid_for((size_t)size * (size / 2) * n_slices, kT);
+    if (complex_elems) f_fftshift_2d<float2><<<g, kT, 0, (cudaStream_t)stream>>>((float2 *)d_data, size, n_slices);
+    else f_fftshift_2d<float><<<g, kT, 0, (cudaStream_t)stream>>>(d_data, size, n_slices);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_fftshift_3d(float *d_data, int complex_elems, int size, void *stream)
+{
+    if (size <= 0 || (size & 1) || !d_data) return GG_ERR_INVALID_ARG;
+    const unsigned g = grid_for((size_t)size * size * (size / 2), kT);
+    if (complex_elems) f_fftshift_3d<float2><<<g, kT, 0, (cudaStream_t)stream>>>((float2 *)d_data, size);
+    else f_fftshift_3d<float><<<g, kT, 0, (cudaStream_t)stream>>>(d_data, size);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_pad_volume(const float *d_in, float *d_out, int in_x, int in_y, int in_z, int pad_x, int pad_y,
+                                    int pad_z, void *stream)
+{
+    if (in_x <= 0 || in_y <= 0 || in_z <= 0 || pad_x < 0 || pad_y < 0 || pad_z < 0 || !d_in || !d_out) return GG_ERR_INVALID_ARG;
+    const size_t c = (size_t)(in_x + 2 * pad_x) * (in_y + 2 * pad_y) * (in_z + 2 * pad_z);
+    f_pad<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>(d_in, d_out, in_x, in_y, in_z, pad_x, pad_y, pad_z);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_crop_volume(const float *d_in, float *d_out, int in_x, int in_y, int in_z, int crop_x, int crop_y,
+                                     int crop_z, void *stream)
+{
+    if (in_x <= 0 || in_y <= 0 || in_z <= 0 || crop_x < 0 || crop_y < 0 || crop_z < 0 || 2 * crop_x >= in_x ||
+        2 * crop_y >= in_y || 2 * crop_z >= in_z || !d_in || !d_out)
+        return GG_ERR_INVALID_ARG;
+    const size_t c = (size_t)(in_x - 2 * crop_x) * (in_y - 2 * crop_y) * (in_z - 2 * crop_z);
+    f_crop<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>(d_in, d_out, in_x, in_y, in_z, crop_x, crop_y, crop_z);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_divide_volumes(float *d_a, const float *d_b, int size, int n_slices, void *stream)
+{
+    if (size <= 0 || n_slices < 0 || !d_a || !d_b) return GG_ERR_INVALID_ARG;
+    const size_t c = slice_count(size, n_slices);
+    f_divide_volumes<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>(d_a, d_b, c);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_multiply_volumes(float *d_a, const float *d_b, int a_complex, int size, int n_slices, void *stream)
+{
+    if (size <= 0 || n_slices < 0 || !d_a || !d_b) return GG_ERR_INVALID_ARG;
+    const size_t c = slice_count(size, n_slices);
+    f_multiply<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>(d_a, d_b, c, a_complex != 0);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_add_volumes(float *d_a, const float *d_b, int size, int n_slices, void *stream)
+{
+    if (size <= 0 || n_slices < 0 || !d_a || !d_b) return GG_ERR_INVALID_ARG;
+    const size_t c = slice_count(size, n_slices);
+    f_add<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>(d_a, d_b, c);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_divide_scalar(float *d_a, float scalar, int size, int n_slices, void *stream)
+{
+    if (size <= 0 || n_slices < 0 || !d_a) return GG_ERR_INVALID_ARG;
+    const size_t c = slice_count(size, n_slices);
+    f_div_scalar<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>(d_a, scalar, c);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_real_to_complex(const float *d_real, float *d_complex, int size, int n_slices, void *stream)
+{
+    if (size <= 0 || n_slices < 0 || !d_real || !d_complex) return GG_ERR_INVALID_ARG;
+    const size_t c = slice_count(size, n_slices);
+    f_real_to_complex<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>(d_real, (float2 *)d_complex, c);
+    GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_complex_to_real(const float *d_complex, float *d_real, int size, int n_slices, void *stream)
+{
+    if (size <= 0 || n_slices < 0 || !d_real || !d_complex) return GG_ERR_INVALID_ARG;
+    const size_t c = slice_count(size, n_slices);
+    f_complex_to_real<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>((const float2 *)d_complex, d_real, c);
+    GG_FILTER_RET();
+}

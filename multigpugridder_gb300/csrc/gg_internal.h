@@ -1,0 +1,96 @@
+// Internal launcher interface shared by the kernel and API translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stddef.h>
+
+namespace gg {
+
+enum Prec { kF32 = 0, kF16 = 1, kBF16 = 2 };
+
+inline size_t prec_bytes(int p) { return p == kF32 ? 4 : 2; }
+
+// Largest KB table accepted (the kernels stage it in shared memory).
+constexpr int kMaxKerSizeHost = 1000;
+
+// Geometry of one projection problem.
+struct Geom {
+    int V;           // CAS volume edge
+    int M;           // CAS image edge
+    int mask_radius; // int, as RunKernel passes it
+    int ker_size;    // KB table length
+    float ker_hw;    // KB half-width (2)
+};
+
+// ---- projection kernels (gg_project.cu) ----------------------------------
+// Forward projection: CAS volume (storage `vprec`) -> CAS images (FP32,
+// n*M*M, zero outside the mask).  `five_taps` selects the reference's full
+// 5x5x5 window (needed only for KB tables whose edge values are not zero).
+// Storage scaling: FP16 storage holds x / scale, with scale a power of two
+// kept in device memory (d_scale; NULL means 1) so no host sync is needed.
+// The forward projection multiplies every output pixel by *d_scale.
+cudaError_t launch_forward_project(const void *d_vol, int vprec, float *d_img, const float *d_ker,
+                                   const float *d_axes, int n, const Geom &g, bool five_taps,
+                                   const float *d_scale, cudaStream_t s);
+
+// Back projection with the reference window rule, accumulated (+=) into the
+// FP32 CAS volume.  d_img holds n*M*M CAS images in storage `iprec`; when
+// `ones` is set the images are taken to be all ones (plane density) and
+// d_img is not read.
+// *d_scale multiplies each voxel's sum before it is added.
+cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, bool ones,
+                                    const float *d_ker, const float *d_axes, int n, const Geom &g,
+                                    const float *d_scale, cudaStream_t s);
+
+// Exact adjoint of launch_forward_project, accumulated into d_vol.
+cudaError_t launch_back_project_adjoint(float *d_vol, const void *d_img, int iprec, const float *d_ker,
+                                        const float *d_axes, int n, const Geom &g, const float *d_scale,
+                                        cudaStream_t s);
+
+// ---- CAS / FFT stages (gg_cas.cu) ------------------------------------------
+// Volume N^3 -> real M^3 FFT input: centred zero-pad, separable precomp
+// multiply, fftshift folded into the index map.
+cudaError_t launch_vol_to_fft_input(const float *d_vol, int N, int M, const double *d_precomp,
+                                    float *d_x, cudaStream_t s);
+// R2C half spectrum [M][M][M/2+1] -> CAS volume V^3 (storage `prec`), border zeroed.
+cudaError_t launch_spectrum_to_cas_volume(const cufftComplex *d_spec, int M, int V, void *d_cas,
+                                          int prec, const float *d_scale, cudaStream_t s);
+// CAS volume V^3 (FP32) -> Hermitian half spectrum for C2R: crop the pad,
+// FromCAS 3-D, fftshift folded into the index map.
+cudaError_t launch_cas_volume_to_spectrum(const float *d_cas, int V, int M, cufftComplex *d_spec,
+                                          cudaStream_t s);
+// C2R output M^3 -> volume N^3: fftshift, 1/M^3, precomp, centred crop.
+cudaError_t launch_fft_output_to_vol(const float *d_y, int M, int N, const double *d_precomp,
+                                     float *d_vol, cudaStream_t s);
+// CAS images n*M*M -> Hermitian half spectra n*M*(M/2+1) (FromCAS 2-D + shift).
+cudaError_t launch_cas_images_to_spectrum(const float *d_cas, int M, int n, cufftComplex *d_spec,
+                                          cudaStream_t s);
+// C2R outputs n*M*M -> images n*N*N (shift, centred crop, 1/M^2).
+cudaError_t launch_fft_output_to_images(const float *d_y, int M, int N, int n, float *d_img,
+                                        cudaStream_t s);
+// Images n*N*N -> R2C inputs n*M*M (centred zero-pad, shift).
+cudaError_t launch_images_to_fft_input(const float *d_img, int N, int M, int n, float *d_x,
+                                       cudaStream_t s);
+// R2C half spectra n*M*(M/2+1) -> CAS images n*M*M (shift, Re+Im) in storage `prec`.
+cudaError_t launch_spectrum_to_cas_images(const cufftComplex *d_spec, int M, int n, void *d_cas,
+                                          int prec, const float *d_scale, cudaStream_t s);
+// a = a / (b + eps) over `count` elements (reconstructVol's plane-density division).
+cudaError_t launch_divide_plane_density(float *d_a, const float *d_b, size_t count, float eps,
+                                        cudaStream_t s);
+// FP32 -> storage conversion (count elements): out = in / *d_scale.
+cudaError_t launch_convert(const float *d_in, void *d_out, int prec, size_t count, const float *d_scale,
+                           cudaStream_t s);
+// *d_scale = smallest power of two >= max|x| / target (at least 1) over
+// `count` floats; d_work is one scratch unsigned int.
+cudaError_t launch_storage_scale(const float *d_x, size_t count, float target, unsigned int *d_work,
+                                 float *d_scale, cudaStream_t s);
+
+// Adds to the process-wide count of kernels launched by this library.
+void count_launches(long long n);
+
+// ---- host math (gg_kb.cpp) --------------------------------------------------
+void kb_table_f64(int hw, int size, double *out);
+void precomp_f64(int M, int hw, double *out);
+
+} // namespace gg

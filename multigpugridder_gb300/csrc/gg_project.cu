@@ -1,0 +1,411 @@
+// Kaiser-Bessel Fourier-slice projection kernels for GB300 (sm_103a).
+//
+//   forward projection   CAS volume -> CAS images (pixel-driven gather)
+//   back projection      CAS images -> CAS volume, reference window rule
+//   adjoint projection   exact adjoint of the forward projection
+//
+// Conventions follow the reference kernels (src/Projection/gpuForwardProject.cu,
+// src/Projection/gpuBackProject.cu): x fastest, CAS-volume centre V/2, image
+// centre M/2, nearest-index lookup into the KB table, int mask radius.
+#include <algorithm>
+
+#include "gg_common.cuh"
+#include "gg_internal.h"
+
+namespace gg {
+
+// ---------------------------------------------------------------------------
+// Shared pieces
+// ---------------------------------------------------------------------------
+
+// Sample point of pixel (di, dj) (offsets from the image centre) in the CAS
+// volume frame, written as the reference writes it (gpuForwardProject.cu:53-55)
+// and shared by the forward and adjoint kernels so both see identical bits.
+__device__ __forceinline__ float sample_coord(float n_x, float n_y, int di, int dj, int vc)
+{
+    return n_x * ((float)di) + n_y * ((float)dj) + (float)vc;
+}
+
+// Callers pass r in [-convW, convW], so the index is already in range; the
+// clamp only keeps a NaN or infinite coordinate (bad axes) inside the table.
+__device__ __forceinline__ float kb_weight(const float *sker, float r, float kerScale, float kerCenter, int kerSize)
+{
+    return sker[min(max(kb_index(r, kerScale, kerCenter), 0), kerSize - 1)];
+}
+
+__device__ __forceinline__ void load_table(float *sker, const float *ker, int kerSize)
+{
+    for (int t = threadIdx.x; t < kerSize; t += blockDim.x) sker[t] = __ldg(ker + t);
+}
+
+static int num_sms()
+{
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+// ---------------------------------------------------------------------------
+// Forward projection
+// ---------------------------------------------------------------------------
+// One CTA = a 16x16 pixel tile of one direction; persistent grid-stride loop
+// over (direction, tile) items, direction-major so that the CTAs resident at
+// any time read the same few slabs of the volume.  Warps cover 8x4 pixel
+// blocks, which keeps a warp's tap addresses compact in the volume.
+//
+// With a KB table whose first and last entries are zero (getKernelFiltTable
+// forces both, getKernelFiltTable.m:12-13), only the 4 taps floor(f)-1 ..
+// floor(f)+2 per axis can carry weight: of the reference's 5 taps around
+// round(f) (gpuForwardProject.cu:63-98) the fifth always has |r| >= 2, is
+// clamped to the table edge and weighs exactly zero.  TAPS = 5 keeps the
+// reference's full window for tables without zero edges.
+constexpr int kFpTile = 16;
+constexpr int kFpThreads = 256;
+
+template <typename TV, int TAPS>
+__global__ void __launch_bounds__(kFpThreads)
+fp_kernel(const TV *__restrict__ vol, int V, float *__restrict__ img, int M,
+          const float *__restrict__ axes, int maskR, const float *__restrict__ ker, int kerSize,
+          float kerHW, int tilesX, long long nItems, const float *__restrict__ d_scale)
+{
+    const float outScale = d_scale ? *d_scale : 1.0f;
+    __shared__ float sker[kMaxKerSize];
+    load_table(sker, ker, kerSize);
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lx = (lane & 7) | ((warp & 1) << 3);
+    const int ly = (lane >> 3) | ((warp >> 1) << 2);
+    const int ic = M / 2, vc = V / 2;
+    const float kerCenter = ((float)kerSize - 1) / 2;
+    const float kerScale = kerCenter / kerHW;
+    const float convW = (float)(int)roundf(kerHW);
+    const long long R2 = (long long)maskR * maskR;
+    const int tilesPerImg = tilesX * tilesX;
+    const size_t VV = (size_t)V * V;
+    const long long V3 = (long long)VV * V;
+
+    for (long long item = blockIdx.x; item < nItems; item += gridDim.x) {
+        const int a = (int)(item / tilesPerImg);
+        const int t = (int)(item - (long long)a * tilesPerImg);
+        const int i = (t % tilesX) * kFpTile + lx;
+        const int j = (t / tilesX) * kFpTile + ly;
+        if (i >= M || j >= M) continue;
+        float *out = img + (size_t)a * M * M + (size_t)j * M + i;
+        const int di = i - ic, dj = j - ic;
+        if ((long long)di * di + (long long)dj * dj > R2) {
+            *out = 0.0f;
+            continue;
+        }
+        const float *ax = axes + 9 * (size_t)a;
+        const float nx0 = __ldg(ax + 0), nx1 = __ldg(ax + 1), nx2 = __ldg(ax + 2);
+        const float ny0 = __ldg(ax + 3), ny1 = __ldg(ax + 4), ny2 = __ldg(ax + 5);
+        const float fi = sample_coord(nx0, ny0, di, dj, vc);
+        const float fj = sample_coord(nx1, ny1, di, dj, vc);
+        const float fk = sample_coord(nx2, ny2, di, dj, vc);
+
+        int b0, b1, b2;
+        float wi[TAPS], wj[TAPS], wk[TAPS];
+        if (TAPS == 4) {
+            b0 = (int)floorf(fi) - 1;
+            b1 = (int)floorf(fj) - 1;
+            b2 = (int)floorf(fk) - 1;
+#pragma unroll
+            for (int d = 0; d < TAPS; d++) {
+                // r lies in (-2, 2] for these taps: no clamp needed
+                wi[d] = kb_weight(sker, (float)(b0 + d) - fi, kerScale, kerCenter, kerSize);
+                wj[d] = kb_weight(sker, (float)(b1 + d) - fj, kerScale, kerCenter, kerSize);
+                wk[d] = kb_weight(sker, (float)(b2 + d) - fk, kerScale, kerCenter, kerSize);
+            }
+        } else {
+            b0 = (int)roundf(fi) - 2;
+            b1 = (int)roundf(fj) - 2;
+            b2 = (int)roundf(fk) - 2;
+#pragma unroll
+            for (int d = 0; d < TAPS; d++) {
+                wi[d] = kb_weight(sker, fminf(fmaxf((float)(b0 + d) - fi, -convW), convW), kerScale, kerCenter, kerSize);
+                wj[d] = kb_weight(sker, fminf(fmaxf((float)(b1 + d) - fj, -convW), convW), kerScale, kerCenter, kerSize);
+                wk[d] = kb_weight(sker, fminf(fmaxf((float)(b2 + d) - fk, -convW), convW), kerScale, kerCenter, kerSize);
+            }
+        }
+
+        float acc = 0.0f;
+        const bool inside = b0 >= 0 && b1 >= 0 && b2 >= 0 && b0 + TAPS <= V && b1 + TAPS <= V && b2 + TAPS <= V;
+        if (inside) {
+            const TV *base = vol + (size_t)b2 * VV + (size_t)b1 * V + b0;
+#pragma unroll
+            for (int dk = 0; dk < TAPS; dk++) {
+#pragma unroll
+                for (int dj2 = 0; dj2 < TAPS; dj2++) {
+                    const TV *p = base + (size_t)dk * VV + (size_t)dj2 * V;
+                    float s = 0.0f;
+#pragma unroll
+                    for (int d = 0; d < TAPS; d++) s = fmaf(wi[d], ld_f32(p + d), s);
+                    acc = fmaf(wj[dj2] * wk[dk], s, acc);
+                }
+            }
+        } else {
+            // Near the volume edge: the reference's linear-index test
+            // (gpuForwardProject.cu:90), plus a lower bound.
+            for (int dk = 0; dk < TAPS; dk++)
+                for (int dj2 = 0; dj2 < TAPS; dj2++)
+                    for (int d = 0; d < TAPS; d++) {
+                        long long lin = (long long)(b2 + dk) * (long long)VV + (long long)(b1 + dj2) * V + (b0 + d);
+                        if (lin >= 0 && lin < V3) acc = fmaf(wi[d] * wj[dj2] * wk[dk], ld_f32(vol + lin), acc);
+                    }
+        }
+        *out = acc * outScale;
+    }
+}
+
+template <typename TV, int TAPS>
+static cudaError_t launch_fp_t(const TV *vol, float *img, const float *ker, const float *axes, int n,
+                               const Geom &g, const float *scale, cudaStream_t s)
+{
+    const int tilesX = (g.M + kFpTile - 1) / kFpTile;
+    const long long nItems = (long long)n * tilesX * tilesX;
+    if (nItems == 0) return cudaSuccess;
+    int perSm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fp_kernel<TV, TAPS>, kFpThreads, 0);
+    if (perSm <= 0) perSm = 1;
+    long long grid = (long long)num_sms() * perSm;
+    if (grid > nItems) grid = nItems;
+    fp_kernel<TV, TAPS><<<(unsigned)grid, kFpThreads, 0, s>>>(vol, g.V, img, g.M, axes, g.mask_radius, ker,
+                                                               g.ker_size, g.ker_hw, tilesX, nItems, scale);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_forward_project(const void *d_vol, int vprec, float *d_img, const float *d_ker,
+                                   const float *d_axes, int n, const Geom &g, bool five_taps, const float *scale,
+                                   cudaStream_t s)
+{
+    if (vprec == kF32)
+        return five_taps ? launch_fp_t<float, 5>((const float *)d_vol, d_img, d_ker, d_axes, n, g, scale, s)
+                         : launch_fp_t<float, 4>((const float *)d_vol, d_img, d_ker, d_axes, n, g, scale, s);
+    if (vprec == kF16)
+        return five_taps ? launch_fp_t<__half, 5>((const __half *)d_vol, d_img, d_ker, d_axes, n, g, scale, s)
+                         : launch_fp_t<__half, 4>((const __half *)d_vol, d_img, d_ker, d_axes, n, g, scale, s);
+    return five_taps ? launch_fp_t<__nv_bfloat16, 5>((const __nv_bfloat16 *)d_vol, d_img, d_ker, d_axes, n, g, scale, s)
+                     : launch_fp_t<__nv_bfloat16, 4>((const __nv_bfloat16 *)d_vol, d_img, d_ker, d_axes, n, g, scale, s);
+}
+
+// ---------------------------------------------------------------------------
+// Back projection, reference window rule
+// ---------------------------------------------------------------------------
+// One CTA owns an 8x8x4 brick of voxels (one voxel per thread) and keeps each
+// voxel's sum in a register, so the volume is written once per launch with a
+// coalesced read-modify-write and no atomics.  Directions are staged through
+// shared memory in chunks; a chunk is first culled against the brick (slab
+// |dot(v - c, z)| <= kerHWidth must reach the brick), then each warp culls
+// against its own 8x4x1 sub-brick, and only then does each voxel apply the
+// reference's per-voxel test and 5x5 window (gpuBackProject.cu:54-107).
+// Directions are visited in order, so each voxel sums its directions in the
+// same order as the reference.
+constexpr int kBpBX = 8, kBpBY = 8, kBpBZ = 4;
+constexpr int kBpThreads = kBpBX * kBpBY * kBpBZ;
+constexpr int kBpChunk = 256;
+static_assert(kBpChunk == kBpThreads, "the cull compaction gives one direction per thread");
+
+// Conservative reach of the slab test: fp32 rounding of f_imgk is far below this.
+constexpr float kCullEps = 1e-2f;
+
+template <typename TI, bool ONES, bool ADJ>
+__global__ void __launch_bounds__(kBpThreads)
+bp_kernel(float *__restrict__ vol, int V, const TI *__restrict__ img, int M,
+          const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
+          float kerHW, int bricksX, int bricksY, const float *__restrict__ d_scale)
+{
+    __shared__ float sker[kMaxKerSize];
+    __shared__ float sax[kBpChunk * 9];
+    __shared__ int slist[kBpChunk];
+    __shared__ int swarp[kBpChunk / 32];
+    __shared__ int scount;
+
+    const int tid = threadIdx.x;
+    const int bxi = blockIdx.x % bricksX;
+    const int byi = (blockIdx.x / bricksX) % bricksY;
+    const int bzi = blockIdx.x / (bricksX * bricksY);
+    const int x0 = bxi * kBpBX, y0 = byi * kBpBY, z0 = bzi * kBpBZ;
+    const int vi = x0 + (tid % kBpBX);
+    const int vj = y0 + (tid / kBpBX) % kBpBY;
+    const int vk = z0 + tid / (kBpBX * kBpBY);
+    const int volCenter = (int)((float)V) / 2;
+    const int imgCenter = (int)((float)M) / 2;
+
+    // Skip bricks that lie entirely outside the mask sphere.
+    {
+        const float cx = fmaxf(fabsf((float)(x0 + (kBpBX - 1) * 0.5f - volCenter)) - 0.5f * (kBpBX - 1), 0.f);
+        const float cy = fmaxf(fabsf((float)(y0 + (kBpBY - 1) * 0.5f - volCenter)) - 0.5f * (kBpBY - 1), 0.f);
+        const float cz = fmaxf(fabsf((float)(z0 + (kBpBZ - 1) * 0.5f - volCenter)) - 0.5f * (kBpBZ - 1), 0.f);
+        // the adjoint also reaches voxels up to 2*sqrt(3) beyond the mask sphere
+        const float reach = ADJ ? (float)maskR + 4.0f : (float)maskR;
+        if (cx * cx + cy * cy + cz * cz > reach * reach + 1.0f) return;
+    }
+
+    load_table(sker, ker, kerSize);
+
+    const long long d2 = (long long)(vi - volCenter) * (vi - volCenter) + (long long)(vj - volCenter) * (vj - volCenter) +
+                         (long long)(vk - volCenter) * (vk - volCenter);
+    const bool active = vi < V && vj < V && vk < V && (ADJ || d2 <= (long long)maskR * maskR);
+
+    const int convW = (int)roundf(kerHW);
+    const float kerCenter = ((float)kerSize - 1) / 2;
+    const float kerScale = kerCenter / kerHW;
+    // reach of the brick / warp sub-brick along the projection direction
+    const float bcx = x0 + 0.5f * (kBpBX - 1) - volCenter, bcy = y0 + 0.5f * (kBpBY - 1) - volCenter,
+                bcz = z0 + 0.5f * (kBpBZ - 1) - volCenter;
+    const int warp = tid >> 5;
+    const float wcx = bcx, wcy = y0 + (warp & 1) * 4 + 1.5f - volCenter, wcz = z0 + (warp >> 1) - volCenter;
+    // slab half-thickness: kerHW for the reference rule; for the adjoint, any
+    // voxel within the 4^3 window of a sample point (|r| < 2 per axis)
+    const float slab = ADJ ? 2.0f * 1.7320508f + kCullEps : kerHW + kCullEps;
+    const int MM = M * M;
+
+    float accAll = 0.0f;
+    for (int c0 = 0; c0 < n; c0 += kBpChunk) {
+        const int cn = min(kBpChunk, n - c0);
+        __syncthreads();
+        for (int t = tid; t < cn * 9; t += kBpThreads) sax[t] = __ldg(axes + (size_t)c0 * 9 + t);
+        __syncthreads();
+        // brick-level cull, compacted in direction order
+        bool keep = false;
+        if (tid < cn) {
+            const float *ax = sax + tid * 9;
+            const float zx = ax[6], zy = ax[7], zz = ax[8];
+            const float d = bcx * zx + bcy * zy + bcz * zz;
+            const float ext = 0.5f * ((kBpBX - 1) * fabsf(zx) + (kBpBY - 1) * fabsf(zy) + (kBpBZ - 1) * fabsf(zz));
+            keep = fabsf(d) <= slab + ext;
+        }
+        const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+        if ((tid & 31) == 0 && tid < kBpChunk) swarp[tid >> 5] = __popc(ballot);
+        __syncthreads();
+        if (tid < kBpChunk) {
+            int off = 0;
+            for (int w = 0; w < (tid >> 5); w++) off += swarp[w];
+            if (keep) slist[off + __popc(ballot & ((1u << (tid & 31)) - 1u))] = tid;
+            if (tid == kBpChunk - 1) {
+                int tot = 0;
+                for (int w = 0; w < kBpChunk / 32; w++) tot += swarp[w];
+                scount = tot;
+            }
+        }
+        __syncthreads();
+        const int count = scount;
+
+        for (int q = 0; q < count; q++) {
+            const int al = slist[q];
+            const float *ax = sax + al * 9;
+            const float nx0 = ax[0], nx1 = ax[1], nx2 = ax[2];
+            const float ny0 = ax[3], ny1 = ax[4], ny2 = ax[5];
+            const float nz0 = ax[6], nz1 = ax[7], nz2 = ax[8];
+            {   // warp-level cull (uniform across the warp)
+                const float d = wcx * nz0 + wcy * nz1 + wcz * nz2;
+                const float ext = 0.5f * ((kBpBX - 1) * fabsf(nz0) + 3.0f * fabsf(nz1));
+                if (fabsf(d) > slab + ext) continue;
+            }
+            if (!active) continue;
+            const TI *img_ptr = img + (size_t)(c0 + al) * MM;
+            if (!ADJ) {
+                // gpuBackProject.cu:62-107
+                const float f_imgi = ((float)vi - volCenter) * nx0 + ((float)vj - volCenter) * nx1 + ((float)vk - volCenter) * nx2 + imgCenter;
+                const float f_imgj = ((float)vi - volCenter) * ny0 + ((float)vj - volCenter) * ny1 + ((float)vk - volCenter) * ny2 + imgCenter;
+                const float f_imgk = ((float)vi - volCenter) * nz0 + ((float)vj - volCenter) * nz1 + ((float)vk - volCenter) * nz2;
+                if (!(fabsf(f_imgk) <= kerHW)) continue;
+                const int imgi = (int)roundf(f_imgi);
+                const int imgj = (int)roundf(f_imgj);
+                float cumSum = 0.0f;
+                for (int j1 = imgj - convW; j1 <= imgj + convW; j1++) {
+                    for (int i1 = imgi - convW; i1 <= imgi + convW; i1++) {
+                        float imgi1 = (i1 - imgCenter) * nx0 + (j1 - imgCenter) * ny0 + volCenter;
+                        float r = fminf(fmaxf((float)imgi1 - vi, (float)-convW), (float)convW);
+                        int kidx = min(max(kb_index(r, kerScale, kerCenter), 0), kerSize - 1);
+                        float w = sker[kidx];
+                        float imgj1 = (i1 - imgCenter) * nx1 + (j1 - imgCenter) * ny1 + volCenter;
+                        r = fminf(fmaxf((float)imgj1 - vj, (float)-convW), (float)convW);
+                        kidx = min(max(kb_index(r, kerScale, kerCenter), 0), kerSize - 1);
+                        w = w * sker[kidx];
+                        float imgk1 = (i1 - imgCenter) * nx2 + (j1 - imgCenter) * ny2 + volCenter;
+                        r = fminf(fmaxf((float)imgk1 - vk, (float)-convW), (float)convW);
+                        kidx = min(max(kb_index(r, kerScale, kerCenter), 0), kerSize - 1);
+                        w = w * sker[kidx];
+                        const int lin = j1 * M + i1;
+                        if (lin < MM && lin >= 0) cumSum += (ONES ? 1.0f : ld_f32(img_ptr + lin)) * w;
+                    }
+                }
+                accAll += cumSum;
+            } else {
+                // Exact adjoint of fp_kernel<., 4>: every pixel whose 4^3
+                // window contains this voxel, with the forward weight.  Such a
+                // pixel lies within 2*sqrt(3) of the voxel's projection.
+                const float pi = ((float)vi - volCenter) * nx0 + ((float)vj - volCenter) * nx1 + ((float)vk - volCenter) * nx2;
+                const float pj = ((float)vi - volCenter) * ny0 + ((float)vj - volCenter) * ny1 + ((float)vk - volCenter) * ny2;
+                const float pk = ((float)vi - volCenter) * nz0 + ((float)vj - volCenter) * nz1 + ((float)vk - volCenter) * nz2;
+                if (!(fabsf(pk) < 2.0f * 1.7320508f + kCullEps)) continue;
+                const int ilo = (int)ceilf(pi - 3.47f), ihi = (int)floorf(pi + 3.47f);
+                const int jlo = (int)ceilf(pj - 3.47f), jhi = (int)floorf(pj + 3.47f);
+                const long long R2 = (long long)maskR * maskR;
+                float s = 0.0f;
+                for (int dj = jlo; dj <= jhi; dj++) {
+                    for (int di = ilo; di <= ihi; di++) {
+                        if ((long long)di * di + (long long)dj * dj > R2) continue;
+                        const int pxi = di + imgCenter, pxj = dj + imgCenter;
+                        if (pxi < 0 || pxi >= M || pxj < 0 || pxj >= M) continue;
+                        const float fi = sample_coord(nx0, ny0, di, dj, volCenter);
+                        const float fj = sample_coord(nx1, ny1, di, dj, volCenter);
+                        const float fk = sample_coord(nx2, ny2, di, dj, volCenter);
+                        // membership in the forward window floor(f)-1 .. floor(f)+2
+                        const int oi = vi - ((int)floorf(fi) - 1), oj = vj - ((int)floorf(fj) - 1), ok = vk - ((int)floorf(fk) - 1);
+                        if ((unsigned)oi > 3u || (unsigned)oj > 3u || (unsigned)ok > 3u) continue;
+                        const float w = kb_weight(sker, (float)vi - fi, kerScale, kerCenter, kerSize) *
+                                        kb_weight(sker, (float)vj - fj, kerScale, kerCenter, kerSize) *
+                                        kb_weight(sker, (float)vk - fk, kerScale, kerCenter, kerSize);
+                        s = fmaf(w, ld_f32(img_ptr + (size_t)pxj * M + pxi), s);
+                    }
+                }
+                accAll += s;
+            }
+        }
+    }
+    if (active) {
+        float *p = vol + (size_t)vk * V * V + (size_t)vj * V + vi;
+        *p = *p + accAll * (d_scale ? *d_scale : 1.0f);
+    }
+}
+
+template <typename TI, bool ONES, bool ADJ>
+static cudaError_t launch_bp_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
+                               const Geom &g, const float *scale, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int bx = (g.V + kBpBX - 1) / kBpBX, by = (g.V + kBpBY - 1) / kBpBY, bz = (g.V + kBpBZ - 1) / kBpBZ;
+    const long long nb = (long long)bx * by * bz;
+    bp_kernel<TI, ONES, ADJ><<<(unsigned)nb, kBpThreads, 0, s>>>(vol, g.V, img, g.M, axes, n, g.mask_radius, ker,
+                                                                 g.ker_size, g.ker_hw, bx, by, scale);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, bool ones, const float *d_ker,
+                                    const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
+{
+    if (ones) return launch_bp_t<float, true, false>(d_vol, nullptr, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF32) return launch_bp_t<float, false, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF16) return launch_bp_t<__half, false, false>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
+    return launch_bp_t<__nv_bfloat16, false, false>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g, scale, s);
+}
+
+cudaError_t launch_back_project_adjoint(float *d_vol, const void *d_img, int iprec, const float *d_ker,
+                                        const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
+{
+    if (iprec == kF32) return launch_bp_t<float, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF16) return launch_bp_t<__half, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
+    return launch_bp_t<__nv_bfloat16, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g, scale, s);
+}
+
+} // namespace gg

@@ -1,0 +1,352 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Tolerance: relative L2 <= 1e-5 for the FP32 path (the bound the reference
+parity is stated in; back-projection summation order differs, so exactness is
+by tolerance).  Pixels outside the mask must be exactly zero.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def dptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def to_dev(a, dev):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
+
+
+def test_axes(n, seed):
+    """Random quaternion directions plus the reference's own axis grid, whose
+    30 degree in-plane rotation puts exact 0.5 entries in the axes (table
+    index ties)."""
+    return np.concatenate([O.quaternion_axes(n, seed), O.create_uniform_axes(2, 4)]).astype(np.float32)
+
+
+test_axes.__test__ = False
+
+
+@pytest.mark.parametrize("N", [16, 32, 64])
+def test_forward_kernel_matches_oracle(cuda, gglib, N):
+    import torch
+
+    p = O.Params(N)
+    rng = np.random.default_rng(100 + N)
+    cas = rng.standard_normal((p.V,) * 3).astype(np.float32)
+    axes = test_axes(12, seed=N)
+    ref = O.fp_ref_f32(cas, axes, p.M, p.mask_radius, p.ker)
+    out = torch.full((len(axes), p.M, p.M), float("nan"), device=cuda)
+    rc = gglib.gg_forward_project_kernel(dptr(to_dev(cas, cuda)), dptr(out), dptr(to_dev(p.ker, cuda)),
+                                         dptr(to_dev(axes, cuda)), 2.0, len(axes), p.V, p.M, 3, p.mask_radius,
+                                         p.ker.size, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    assert O.rel_l2(got, ref) < TOL
+    assert np.all(got[ref == 0] == 0)  # outside the mask
+
+
+@pytest.mark.parametrize("N", [16, 32, 64])
+def test_back_kernel_matches_oracle(cuda, gglib, N):
+    import torch
+
+    p = O.Params(N)
+    rng = np.random.default_rng(200 + N)
+    # full-frame random CAS images: border pixels exercise the reference's
+    # row-wrap of windows that cross an image edge (gpuBackProject.cu:99)
+    img = rng.standard_normal((14, p.M, p.M)).astype(np.float32)
+    axes = test_axes(6, seed=N + 1)[:14]
+    ref = O.bp_ref_f32(img, axes, p.V, p.mask_radius, p.ker)
+    vol = torch.zeros((p.V,) * 3, device=cuda)
+    rc = gglib.gg_back_project_kernel(dptr(vol), dptr(to_dev(img, cuda)), dptr(to_dev(p.ker, cuda)),
+                                      dptr(to_dev(axes, cuda)), 2.0, len(axes), p.V, p.M, p.mask_radius, p.ker.size,
+                                      3, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    got = vol.cpu().numpy()
+    assert O.rel_l2(got, ref) < TOL
+    assert np.all(got[ref == 0] == 0)
+
+
+@pytest.mark.parametrize("N", [16, 32])
+def test_adjoint_kernel_is_exact_adjoint(cuda, gglib, N):
+    import torch
+
+    p = O.Params(N)
+    rng = np.random.default_rng(300 + N)
+    x = rng.standard_normal((p.V,) * 3).astype(np.float32)
+    axes = test_axes(8, seed=N + 2)
+    n = len(axes)
+    y = rng.standard_normal((n, p.M, p.M)).astype(np.float32)
+    d_ker, d_axes = to_dev(p.ker, cuda), to_dev(axes, cuda)
+    px = torch.zeros((n, p.M, p.M), device=cuda)
+    assert gglib.gg_forward_project_kernel(dptr(to_dev(x, cuda)), dptr(px), dptr(d_ker), dptr(d_axes), 2.0, n, p.V,
+                                           p.M, 3, p.mask_radius, p.ker.size, None) == 0
+    bty = torch.zeros((p.V,) * 3, device=cuda)
+    assert gglib.gg_back_project_adjoint_kernel(dptr(bty), dptr(to_dev(y, cuda)), dptr(d_ker), dptr(d_axes), 2.0, n,
+                                                p.V, p.M, p.mask_radius, p.ker.size, None) == 0
+    torch.cuda.synchronize()
+    px, bty = px.cpu().numpy().astype(np.float64), bty.cpu().numpy().astype(np.float64)
+    lhs = float(np.sum(px * y))
+    rhs = float(np.sum(x * bty))
+    assert abs(lhs - rhs) <= 1e-5 * max(abs(lhs), np.linalg.norm(px) * np.linalg.norm(y) * 1e-3)
+    ref = O.bp_adjoint_f64(y.astype(np.float64), axes, p.V, p.mask_radius, p.ker)
+    assert O.rel_l2(bty, ref) < TOL
+
+
+def test_reference_rule_is_not_adjoint(cuda, gglib):
+    """The reference's BP window differs from the forward window at general
+    orientations: the two modes must give different volumes."""
+    import torch
+
+    p = O.Params(16)
+    rng = np.random.default_rng(7)
+    axes = O.quaternion_axes(6, seed=8).astype(np.float32)
+    y = rng.standard_normal((6, p.M, p.M)).astype(np.float32)
+    d = [torch.zeros((p.V,) * 3, device=cuda) for _ in range(2)]
+    args = (dptr(to_dev(y, cuda)), dptr(to_dev(p.ker, cuda)), dptr(to_dev(axes, cuda)), 2.0, 6, p.V, p.M,
+            p.mask_radius, p.ker.size)
+    assert gglib.gg_back_project_kernel(dptr(d[0]), *args, 3, None) == 0
+    assert gglib.gg_back_project_adjoint_kernel(dptr(d[1]), *args, None) == 0
+    torch.cuda.synchronize()
+    assert O.rel_l2(d[0].cpu().numpy(), d[1].cpu().numpy()) > 1e-3
+
+
+# ---------------------------------------------------------------------------
+# Whole-path calls through the gridder object
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("N", [16, 32])
+def test_set_volume_cas_prep(cuda, N):
+    import multigpugridder_gb300 as gg
+
+    vol = O.blob_volume(N, 8, seed=N)
+    with gg.MultiGPUGridder(N, 4, adjustInterpFactor=False) as g:
+        g.setVolume(vol)
+        cas = g.getCASVolume()
+    ref = O.cas_from_vol(vol.astype(np.float64))
+    assert O.rel_l2(cas, ref) < TOL
+    p = O.Params(N)
+    border = np.ones((p.V,) * 3, bool)
+    border[3:-3, 3:-3, 3:-3] = False
+    assert np.all(cas[border] == 0)
+
+
+@pytest.mark.parametrize("N", [16, 32])
+def test_get_volume_inverts_cas_prep(cuda, N):
+    import multigpugridder_gb300 as gg
+
+    vol = O.blob_volume(N, 8, seed=N + 5)
+    rng = np.random.default_rng(N)
+    p = O.Params(N)
+    cas = rng.standard_normal((p.V,) * 3).astype(np.float32)
+    with gg.MultiGPUGridder(N, 4, adjustInterpFactor=False) as g:
+        g.setCASVolume(cas)
+        got = g.getVol()
+        g.setVolume(vol)
+        rt = g.getVol()
+    assert O.rel_l2(got, O.vol_from_cas(cas, N)) < TOL
+    assert O.rel_l2(rt, O.vol_from_cas(O.cas_from_vol(vol), N)) < TOL
+
+
+@pytest.mark.parametrize("N,batch", [(32, 1000), (32, 7)])
+def test_forward_project_images(cuda, N, batch):
+    import multigpugridder_gb300 as gg
+
+    p = O.Params(N)
+    vol = O.blob_volume(N, 10, seed=N + 3)
+    axes = test_axes(17, seed=N + 4)
+    with gg.MultiGPUGridder(N, len(axes), adjustInterpFactor=False, MaxAxesToAllocate=batch) as g:
+        g.setVolume(vol)
+        imgs = g.forwardProject(axes)
+        cas = g.forwardProjectCAS(axes)
+    ref_cas = O.fp_ref_f32(O.cas_from_vol(vol).astype(np.float32), axes, p.M, p.mask_radius, p.ker)
+    assert O.rel_l2(cas, ref_cas) < TOL
+    ref = O.imgs_from_cas_imgs(ref_cas.astype(np.float64), N)
+    assert O.rel_l2(imgs, ref) < TOL
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_back_project_images(cuda, pinned):
+    import torch
+
+    import multigpugridder_gb300 as gg
+
+    N = 32
+    p = O.Params(N)
+    rng = np.random.default_rng(5)
+    axes = test_axes(20, seed=9)
+    imgs = rng.standard_normal((len(axes), N, N)).astype(np.float32)
+    if pinned:
+        t = torch.from_numpy(imgs).pin_memory()
+        imgs_in = t.numpy()
+    else:
+        imgs_in = imgs
+    with gg.MultiGPUGridder(N, len(axes), adjustInterpFactor=False, MaxAxesToAllocate=9) as g:
+        g.backProject(imgs_in, axes)
+        got = g.getCASVolume()
+    ref = O.bp_ref_f32(O.cas_imgs_from_imgs(imgs, p.M).astype(np.float32), axes, p.V, p.mask_radius, p.ker)
+    assert O.rel_l2(got, ref) < TOL
+
+
+def test_forward_project_pinned_outputs(cuda):
+    import torch
+
+    import multigpugridder_gb300 as gg
+    from multigpugridder_gb300._lib import lib
+
+    N = 16
+    vol = O.blob_volume(N, 5, seed=1)
+    axes = test_axes(9, seed=2)
+    with gg.MultiGPUGridder(N, len(axes), adjustInterpFactor=False, MaxAxesToAllocate=4) as g:
+        g.setVolume(vol)
+        ref = g.forwardProject(axes)
+        out = torch.empty((len(axes), N, N), dtype=torch.float32).pin_memory()
+        cas = torch.empty((len(axes), g.M, g.M), dtype=torch.float32).pin_memory()
+        a = np.ascontiguousarray(axes, dtype=np.float32)
+        rc = lib().gg_forward_project(g.handle, ctypes.c_void_p(a.ctypes.data), len(axes),
+                                      ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(cas.data_ptr()))
+        assert rc == 0
+        assert np.array_equal(out.numpy(), ref)
+        assert np.array_equal(cas.numpy(), g.forwardProjectCAS(axes))
+
+
+def test_reconstruct_volume(cuda):
+    import multigpugridder_gb300 as gg
+
+    N = 32
+    p = O.Params(N)
+    vol = O.blob_volume(N, 10, seed=21)
+    axes = test_axes(30, seed=22)
+    with gg.MultiGPUGridder(N, len(axes), adjustInterpFactor=False) as g:
+        g.setVolume(vol)
+        imgs = g.forwardProject(axes)
+        rec = g.reconstructVol(imgs, axes)
+    ref, _, _ = O.reconstruct_vol(imgs, axes, p, precision="f32")
+    assert O.rel_l2(rec, ref) < TOL
+
+
+def test_fp_sphere_known_answer(cuda):
+    """ForwardProjectTests.m:28-69: a fuzzy sphere projects to sum(V, 3) in
+    every direction; max |mean(image - GT)| <= 1."""
+    import multigpugridder_gb300 as gg
+
+    N = 64
+    vol = O.fuzzymask(N, 3, N * 0.25, 2, (N // 2 + 1) * np.ones(3)).astype(np.float32)
+    axes = O.create_uniform_axes(10, 50)
+    with gg.MultiGPUGridder(N, len(axes), adjustInterpFactor=False) as g:
+        g.setVolume(vol)
+        imgs = g.forwardProject(axes)
+    gt = vol.astype(np.float64).sum(axis=0)
+    md = (imgs - gt[None]).reshape(len(axes), -1).mean(axis=1)
+    assert np.max(np.abs(md)) <= 1.0
+    assert np.max(np.abs(imgs - gt[None])) < 0.1
+
+
+def test_reconstruction_known_answer(cuda):
+    """BackProjectTests.m:25-66: 128^3 fuzzy sphere, 100x50 directions,
+    forward project -> reconstructVol; max |recon - V| <= 1."""
+    import multigpugridder_gb300 as gg
+
+    N = 128
+    vol = O.fuzzymask(N, 3, N * 0.25, 2, (N // 2 + 1) * np.ones(3)).astype(np.float32)
+    axes = O.create_uniform_axes(100, 50)
+    with gg.MultiGPUGridder(N, len(axes), adjustInterpFactor=False) as g:
+        g.setVolume(vol)
+        imgs = g.forwardProject(axes)
+        g.resetVolume()
+        rec = g.reconstructVol(imgs, axes)
+    assert np.max(np.abs(rec - vol)) <= 1.0
+
+
+def test_zero_axes_and_errors(cuda):
+    import multigpugridder_gb300 as gg
+    from multigpugridder_gb300._lib import GG_ERR_INVALID_ARG, GG_ERR_STATE, GridderError, lib
+
+    N = 16
+    with gg.MultiGPUGridder(N, 4, adjustInterpFactor=False) as g:
+        # forward projection before any volume: state error, not a crash
+        with pytest.raises(GridderError) as e:
+            g._call("gg_forward_project", ctypes.c_void_p(np.zeros(9, np.float32).ctypes.data), 1,
+                    ctypes.c_void_p(np.zeros(N * N, np.float32).ctypes.data), None)
+        assert e.value.code == GG_ERR_STATE
+        g.setVolume(O.blob_volume(N, 3, seed=1))
+        out = g.forwardProject(np.zeros((0, 9), np.float32))
+        assert out.shape == (0, N, N)
+        with pytest.raises(GridderError) as e:
+            g.setVolume(np.zeros((N + 2,) * 3, np.float32))
+        assert e.value.code == GG_ERR_INVALID_ARG
+        with pytest.raises(GridderError):
+            g.set_precision(7)
+    h = ctypes.c_void_p()
+    assert lib().gg_create(15, 1, ctypes.c_float(2.0), 3, 1, None, 1, 0, ctypes.byref(h)) == GG_ERR_INVALID_ARG
+
+
+# ---------------------------------------------------------------------------
+# The reference's own kernels (compiled from its sources into oracle/_ref)
+# ---------------------------------------------------------------------------
+
+
+def _ref():
+    from oracle import ref_kernels
+
+    if not ref_kernels.available():
+        pytest.skip("reference cubins not present")
+    return ref_kernels.RefKernels()
+
+
+@pytest.mark.parametrize("N", [32, 64])
+def test_forward_matches_reference_kernel(cuda, gglib, N):
+    import torch
+
+    rk = _ref()
+    p = O.Params(N)
+    vol = O.blob_volume(N, 12, seed=N + 40)
+    cas = O.cas_from_vol(vol).astype(np.float32)
+    axes = test_axes(24, seed=N + 41)
+    d_cas, d_ker, d_axes = to_dev(cas, cuda), to_dev(p.ker, cuda), to_dev(axes, cuda)
+    ref = torch.zeros((len(axes), p.M, p.M), device=cuda)
+    rk.forward_project(d_cas.data_ptr(), p.V, ref.data_ptr(), p.M, d_axes.data_ptr(), len(axes), p.mask_radius,
+                       d_ker.data_ptr(), p.ker.size)
+    got = torch.full_like(ref, float("nan"))
+    assert gglib.gg_forward_project_kernel(dptr(d_cas), dptr(got), dptr(d_ker), dptr(d_axes), 2.0, len(axes), p.V,
+                                           p.M, 3, p.mask_radius, p.ker.size, None) == 0
+    torch.cuda.synchronize()
+    ref, got = ref.cpu().numpy(), got.cpu().numpy()
+    assert O.rel_l2(got, ref) < TOL
+    # and the oracle restatement agrees with the reference kernel
+    assert O.rel_l2(O.fp_ref_f32(cas, axes, p.M, p.mask_radius, p.ker), ref) < TOL
+
+
+@pytest.mark.parametrize("N", [32, 64])
+def test_back_matches_reference_kernel(cuda, gglib, N):
+    import torch
+
+    rk = _ref()
+    p = O.Params(N)
+    rng = np.random.default_rng(N + 50)
+    img = rng.standard_normal((16, p.M, p.M)).astype(np.float32)
+    axes = test_axes(8, seed=N + 51)[:16]
+    d_img, d_ker, d_axes = to_dev(img, cuda), to_dev(p.ker, cuda), to_dev(axes, cuda)
+    ref = torch.zeros((p.V,) * 3, device=cuda)
+    rk.back_project(ref.data_ptr(), p.V, d_img.data_ptr(), p.M, d_axes.data_ptr(), len(axes), p.mask_radius,
+                    d_ker.data_ptr(), p.ker.size)
+    got = torch.zeros_like(ref)
+    assert gglib.gg_back_project_kernel(dptr(got), dptr(d_img), dptr(d_ker), dptr(d_axes), 2.0, len(axes), p.V, p.M,
+                                        p.mask_radius, p.ker.size, 3, None) == 0
+    torch.cuda.synchronize()
+    ref, got = ref.cpu().numpy(), got.cpu().numpy()
+    assert O.rel_l2(got, ref) < TOL
+    assert O.rel_l2(O.bp_ref_f32(img, axes, p.V, p.mask_radius, p.ker), ref) < TOL
