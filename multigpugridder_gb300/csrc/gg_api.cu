@@ -350,8 +350,10 @@ void fp_batch(gg_gridder *h, const float *d_axes, int b, float *cas_out, float *
 }
 
 // Back-project b directions: images (device, FFT path) or CAS images (device).
+// With `pd`, the plane density of the same directions is accumulated into pd
+// as well (fused into the same kernel for the reference rule).
 void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const float *casimg, float *target, bool ones,
-              int sl, cudaStream_t s)
+              int sl, cudaStream_t s, float *pd = nullptr)
 {
     auto &S = h->slot[sl];
     const void *src = nullptr;
@@ -385,11 +387,23 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
     }
     if (ones) iprec = kF32;
     ProfScope ps(h, s, ones ? GG_KERNEL_DENSITY : GG_KERNEL_BACK);
-    if (h->bp_mode == GG_BP_ADJOINT && !ones)
+    if (h->bp_mode == GG_BP_ADJOINT && !ones) {
         GG_CK(launch_back_project_adjoint(target, src, iprec, h->ker.p, d_axes, b, h->geom(), scale, s));
-    else
+    } else if (pd && !ones) {
+        GG_CK(launch_back_project_ref_density(target, pd, src, iprec, h->ker.p, d_axes, b, h->geom(), scale, s));
+        pd = nullptr;
+    } else {
         GG_CK(launch_back_project_ref(target, src, iprec, ones, h->ker.p, d_axes, b, h->geom(), scale, s));
+    }
     ps.done();
+    if (pd) {
+        // adjoint rule: the plane density is the adjoint applied to all-ones CAS images
+        const size_t MM = (size_t)h->M * h->M;
+        ProfScope pd_ps(h, s, GG_KERNEL_DENSITY);
+        GG_CK(launch_fill(S.casimg.p, MM * b, 1.0f, s));
+        GG_CK(launch_back_project_adjoint(pd, S.casimg.p, kF32, h->ker.p, d_axes, b, h->geom(), nullptr, s));
+        pd_ps.done();
+    }
 }
 
 void upload_axes(gg_gridder *h, const float *axes, int n, cudaStream_t s)
@@ -465,7 +479,7 @@ void fp_host(gg_gridder *h, const float *axes, int n, float *images_out, float *
 // Back projection with host inputs: batch c is copied in on the copy stream
 // (staged when pageable) while batch c-1 is transformed and back-projected.
 void bp_host(gg_gridder *h, const float *axes, int n, const float *images, const float *casimgs, float *target,
-             bool ones)
+             bool ones, float *pd = nullptr)
 {
     cudaStream_t cs = h->cs, cp = h->cp;
     upload_axes(h, axes, n, cs);
@@ -495,7 +509,7 @@ void bp_host(gg_gridder *h, const float *axes, int n, const float *images, const
             GG_CK(cudaStreamWaitEvent(cs, S.ev_free, 0));
         }
         bp_batch(h, h->axes.p + (size_t)a0 * 9, b, casimgs ? nullptr : dbuf, casimgs ? dbuf : nullptr, target, ones, sl,
-                 cs);
+                 cs, pd);
         GG_CK(cudaEventRecord(S.ev_ready, cs));
     }
     GG_CK(cudaStreamSynchronize(cs));
@@ -861,14 +875,9 @@ extern "C" int gg_reconstruct_volume(gg_gridder *h, const float *axes, int n_axe
         h->pd.ensure(V3);
         GG_CK(cudaMemsetAsync(h->cas.p, 0, V3 * sizeof(float), h->cs));
         GG_CK(cudaMemsetAsync(h->pd.p, 0, V3 * sizeof(float), h->cs));
-        if (n_axes > 0) {
-            bp_host(h, axes, n_axes, images, nullptr, h->cas.p, false);
-            // plane density: the same directions with all-ones CAS images
-            for (int a0 = 0; a0 < n_axes; a0 += h->max_batch) {
-                const int b = std::min(h->max_batch, n_axes - a0);
-                bp_batch(h, h->axes.p + (size_t)a0 * 9, b, nullptr, nullptr, h->pd.p, true, 0, h->cs);
-            }
-        }
+        // back projection of the images and, in the same pass, the plane
+        // density (the same directions with all-ones CAS images)
+        if (n_axes > 0) bp_host(h, axes, n_axes, images, nullptr, h->cas.p, false, h->pd.p);
         GG_CK(launch_divide_plane_density(h->cas.p, h->pd.p, V3, 1e-6f, h->cs));
         h->vol_io.ensure(N3);
         do_get_volume(h, h->cas.p, h->vol_io.p, h->cs);
@@ -997,8 +1006,7 @@ extern "C" int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int
         for (int a0 = 0; a0 < n_axes; a0 += B) {
             const int b = std::min(B, n_axes - a0);
             ensure_slot(h, 0, B, false);
-            bp_batch(h, d_axes + (size_t)a0 * 9, b, d_images + (size_t)a0 * NN, nullptr, h->cas.p, false, 0, s);
-            bp_batch(h, d_axes + (size_t)a0 * 9, b, nullptr, nullptr, h->pd.p, true, 0, s);
+            bp_batch(h, d_axes + (size_t)a0 * 9, b, d_images + (size_t)a0 * NN, nullptr, h->cas.p, false, 0, s, h->pd.p);
         }
         GG_CK(launch_divide_plane_density(h->cas.p, h->pd.p, V3, 1e-6f, s));
         do_get_volume(h, h->cas.p, d_volume_out, s);

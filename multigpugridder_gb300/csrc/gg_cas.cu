@@ -309,6 +309,19 @@ cudaError_t launch_spectrum_to_cas_images(const cufftComplex *d_spec, int M, int
     return cudaGetLastError();
 }
 
+__global__ void fill_kernel(float *__restrict__ d, size_t count, float value)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
+        d[e] = value;
+}
+
+cudaError_t launch_fill(float *d, size_t count, float value, cudaStream_t s)
+{
+    fill_kernel<<<grid_for(count, kT), kT, 0, s>>>(d, count, value);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_divide_plane_density(float *d_a, const float *d_b, size_t count, float eps, cudaStream_t s)
 {
     divide_plane_density_kernel<<<grid_for(count, kT), kT, 0, s>>>(d_a, d_b, count, eps);

@@ -22,12 +22,4 @@ template <> __device__ __forceinline__ float from_f32<float>(float x) { return x
 template <> __device__ __forceinline__ __half from_f32<__half>(float x) { return __float2half_rn(x); }
 template <> __device__ __forceinline__ __nv_bfloat16 from_f32<__nv_bfloat16>(float x) { return __float2bfloat16_rn(x); }
 
-// Table index of the reference's nearest-index KB lookup,
-// kerIndex = roundf(r * kerScale + kerCenter) (gpuForwardProject.cu:65-68),
-// for r already inside [-convW, convW] so the index lies in [0, kerSize-1].
-__device__ __forceinline__ int kb_index(float r, float kerScale, float kerCenter)
-{
-    return (int)roundf(r * kerScale + kerCenter);
-}
-
 } // namespace gg

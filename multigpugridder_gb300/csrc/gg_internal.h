@@ -43,6 +43,12 @@ cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, 
                                     const float *d_ker, const float *d_axes, int n, const Geom &g,
                                     const float *d_scale, cudaStream_t s);
 
+// Reference-rule back projection of d_img into d_vol and, in the same pass,
+// of all-ones images (the plane density) into d_pd; both accumulated.
+cudaError_t launch_back_project_ref_density(float *d_vol, float *d_pd, const void *d_img, int iprec,
+                                            const float *d_ker, const float *d_axes, int n, const Geom &g,
+                                            const float *d_scale, cudaStream_t s);
+
 // Exact adjoint of launch_forward_project, accumulated into d_vol.
 cudaError_t launch_back_project_adjoint(float *d_vol, const void *d_img, int iprec, const float *d_ker,
                                         const float *d_axes, int n, const Geom &g, const float *d_scale,
@@ -75,6 +81,8 @@ cudaError_t launch_images_to_fft_input(const float *d_img, int N, int M, int n, 
 // R2C half spectra n*M*(M/2+1) -> CAS images n*M*M (shift, Re+Im) in storage `prec`.
 cudaError_t launch_spectrum_to_cas_images(const cufftComplex *d_spec, int M, int n, void *d_cas,
                                           int prec, const float *d_scale, cudaStream_t s);
+// d[0..count) = value.
+cudaError_t launch_fill(float *d, size_t count, float value, cudaStream_t s);
 // a = a / (b + eps) over `count` elements (reconstructVol's plane-density division).
 cudaError_t launch_divide_plane_density(float *d_a, const float *d_b, size_t count, float eps,
                                         cudaStream_t s);

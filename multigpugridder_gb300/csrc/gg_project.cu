@@ -19,18 +19,32 @@ namespace gg {
 // ---------------------------------------------------------------------------
 
 // Sample point of pixel (di, dj) (offsets from the image centre) in the CAS
-// volume frame, written as the reference writes it (gpuForwardProject.cu:53-55)
-// and shared by the forward and adjoint kernels so both see identical bits.
+// volume frame: the reference's nx*di + ny*dj + volCenter
+// (gpuForwardProject.cu:53-55) as its build evaluates it, fma(nx, di, ny*dj) +
+// vc, written with round-to-nearest intrinsics so the grouping cannot change.
+// Shared by the forward and adjoint kernels so both see identical bits.
 __device__ __forceinline__ float sample_coord(float n_x, float n_y, int di, int dj, int vc)
 {
-    return n_x * ((float)di) + n_y * ((float)dj) + (float)vc;
+    return __fadd_rn(__fmaf_rn(n_x, (float)di, __fmul_rn(n_y, (float)dj)), (float)vc);
 }
 
-// Callers pass r in [-convW, convW], so the index is already in range; the
-// clamp only keeps a NaN or infinite coordinate (bad axes) inside the table.
-__device__ __forceinline__ float kb_weight(const float *sker, float r, float kerScale, float kerCenter, int kerSize)
+// A voxel's image-frame coordinate (gpuBackProject.cu:62-64),
+// fma(a2, n2, fma(a0, n0, a1*n1)); every grouping of the three products gave
+// the same results against the reference kernel, this one is fixed here.
+__device__ __forceinline__ float voxel_proj(float a0, float a1, float a2, float n0, float n1, float n2)
 {
-    return sker[min(max(kb_index(r, kerScale, kerCenter), 0), kerSize - 1)];
+    return __fmaf_rn(a2, n2, __fmaf_rn(a0, n0, __fmul_rn(a1, n1)));
+}
+
+// Table lookup of the reference's nearest-index KB rule,
+// ker[roundf(fma(r, kerScale, kerCenter))], as floor(fma(r, kerScale,
+// kerCenter + 1/2)): equal for every float r in [-2, 2] (checked
+// exhaustively) and one conversion instead of a roundf and a conversion.
+// Callers pass r in [-2, 2]; the clamp only keeps a NaN or infinite
+// coordinate (bad axes) inside the table.
+__device__ __forceinline__ float kb_weight(const float *sker, float r, float kerScale, float kerCenterHalf, int kerSize)
+{
+    return sker[min(max(__float2int_rd(__fmaf_rn(r, kerScale, kerCenterHalf)), 0), kerSize - 1)];
 }
 
 __device__ __forceinline__ void load_table(float *sker, const float *ker, int kerSize)
@@ -84,6 +98,7 @@ fp_kernel(const TV *__restrict__ vol, int V, float *__restrict__ img, int M,
     const int ic = M / 2, vc = V / 2;
     const float kerCenter = ((float)kerSize - 1) / 2;
     const float kerScale = kerCenter / kerHW;
+    const float kerCenterHalf = kerCenter + 0.5f;
     const float convW = (float)(int)roundf(kerHW);
     const long long R2 = (long long)maskR * maskR;
     const int tilesPerImg = tilesX * tilesX;
@@ -118,9 +133,9 @@ fp_kernel(const TV *__restrict__ vol, int V, float *__restrict__ img, int M,
 #pragma unroll
             for (int d = 0; d < TAPS; d++) {
                 // r lies in (-2, 2] for these taps: no clamp needed
-                wi[d] = kb_weight(sker, (float)(b0 + d) - fi, kerScale, kerCenter, kerSize);
-                wj[d] = kb_weight(sker, (float)(b1 + d) - fj, kerScale, kerCenter, kerSize);
-                wk[d] = kb_weight(sker, (float)(b2 + d) - fk, kerScale, kerCenter, kerSize);
+                wi[d] = kb_weight(sker, (float)(b0 + d) - fi, kerScale, kerCenterHalf, kerSize);
+                wj[d] = kb_weight(sker, (float)(b1 + d) - fj, kerScale, kerCenterHalf, kerSize);
+                wk[d] = kb_weight(sker, (float)(b2 + d) - fk, kerScale, kerCenterHalf, kerSize);
             }
         } else {
             b0 = (int)roundf(fi) - 2;
@@ -128,9 +143,9 @@ fp_kernel(const TV *__restrict__ vol, int V, float *__restrict__ img, int M,
             b2 = (int)roundf(fk) - 2;
 #pragma unroll
             for (int d = 0; d < TAPS; d++) {
-                wi[d] = kb_weight(sker, fminf(fmaxf((float)(b0 + d) - fi, -convW), convW), kerScale, kerCenter, kerSize);
-                wj[d] = kb_weight(sker, fminf(fmaxf((float)(b1 + d) - fj, -convW), convW), kerScale, kerCenter, kerSize);
-                wk[d] = kb_weight(sker, fminf(fmaxf((float)(b2 + d) - fk, -convW), convW), kerScale, kerCenter, kerSize);
+                wi[d] = kb_weight(sker, fminf(fmaxf((float)(b0 + d) - fi, -convW), convW), kerScale, kerCenterHalf, kerSize);
+                wj[d] = kb_weight(sker, fminf(fmaxf((float)(b1 + d) - fj, -convW), convW), kerScale, kerCenterHalf, kerSize);
+                wk[d] = kb_weight(sker, fminf(fmaxf((float)(b2 + d) - fk, -convW), convW), kerScale, kerCenterHalf, kerSize);
             }
         }
 
@@ -215,9 +230,64 @@ static_assert(kBpChunk == kBpThreads, "the cull compaction gives one direction p
 // Conservative reach of the slab test: fp32 rounding of f_imgk is far below this.
 constexpr float kCullEps = 1e-2f;
 
-template <typename TI, bool ONES, bool ADJ>
+struct RefWindow {
+    float nx0, nx1, nx2, ny0, ny1, ny2; // direction columns x, y
+    float vi, vj, vk;                   // voxel coordinates
+    float vc;                           // volume centre
+    float kerScale, kerCenterHalf;      // index = floor(r*kerScale + kerCenter + 1/2)
+};
+
+// Pixel (i1, j1)'s position along one volume axis, as the reference's build
+// evaluates `(i1 - imgCenter) * nx + (j1 - imgCenter) * ny + volCenter`
+// (gpuBackProject.cu:77,84,91): fma(pi, nx, pj*ny) + vc, identified by
+// replaying the reference kernel's outputs.  Written with round-to-nearest
+// intrinsics so no unrolling or hoisting can change which product is fused.
+__device__ __forceinline__ float ref_pixel_pos(float pi, float pj, float n_x, float n_y, float vc)
+{
+    return __fadd_rn(__fmaf_rn(pi, n_x, __fmul_rn(pj, n_y)), vc);
+}
+
+// One voxel's 5x5 pixel window under the reference rule (gpuBackProject.cu:74-104),
+// unrolled.  The table index floor(fma(r, kerScale, kerCenter + 1/2)) equals
+// the reference's roundf(fma(r, kerScale, kerCenter)) for every float r in
+// [-2, 2] (checked exhaustively): both round the same exact value once.
+// INSIDE: the whole window lies in the image, so the reference's
+// linear-index test always passes.
+template <typename TI, bool ONES, bool DENS, bool INSIDE>
+__device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker, const TI *__restrict__ img_ptr, int M,
+                                           int imgi, int imgj, int imgCenter, float &cumSum, float &cumW)
+{
+#pragma unroll
+    for (int jo = -2; jo <= 2; jo++) {
+        const int j1 = imgj + jo;
+        const float pj = (float)(j1 - imgCenter);
+#pragma unroll
+        for (int io = -2; io <= 2; io++) {
+            const int i1 = imgi + io;
+            const float pi = (float)(i1 - imgCenter);
+            float r = fminf(fmaxf(ref_pixel_pos(pi, pj, q.nx0, q.ny0, q.vc) - q.vi, -2.0f), 2.0f);
+            float w = sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf))];
+            r = fminf(fmaxf(ref_pixel_pos(pi, pj, q.nx1, q.ny1, q.vc) - q.vj, -2.0f), 2.0f);
+            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf))]);
+            r = fminf(fmaxf(ref_pixel_pos(pi, pj, q.nx2, q.ny2, q.vc) - q.vk, -2.0f), 2.0f);
+            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf))]);
+            const int lin = j1 * M + i1;
+            if (INSIDE || (lin < M * M && lin >= 0)) {
+                // cumSum += img * w, fused as the reference's build fuses it
+                cumSum = __fmaf_rn(ONES ? 1.0f : ld_f32(img_ptr + lin), w, cumSum);
+                if (DENS) cumW = __fadd_rn(cumW, w);
+            }
+        }
+    }
+}
+
+// DENS: also accumulate the plane density -- the back projection of
+// all-ones CAS images over the same directions (reconstructVol,
+// MultiGPUGridder_Matlab_Class.m:300-304) -- into `pd`.  Both sums use the
+// same weights, so one pass does the work of the reference's two.
+template <typename TI, bool ONES, bool ADJ, bool DENS>
 __global__ void __launch_bounds__(kBpThreads)
-bp_kernel(float *__restrict__ vol, int V, const TI *__restrict__ img, int M,
+bp_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
           const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
           float kerHW, int bricksX, int bricksY, const float *__restrict__ d_scale)
 {
@@ -232,9 +302,14 @@ bp_kernel(float *__restrict__ vol, int V, const TI *__restrict__ img, int M,
     const int byi = (blockIdx.x / bricksX) % bricksY;
     const int bzi = blockIdx.x / (bricksX * bricksY);
     const int x0 = bxi * kBpBX, y0 = byi * kBpBY, z0 = bzi * kBpBZ;
-    const int vi = x0 + (tid % kBpBX);
-    const int vj = y0 + (tid / kBpBX) % kBpBY;
-    const int vk = z0 + tid / (kBpBX * kBpBY);
+    // each warp owns a compact 4x4x2 block of the brick: a small extent along
+    // any projection direction, so fewer lanes sit outside the slab when the
+    // warp is inside it
+    const int warp = tid >> 5, lane = tid & 31;
+    const int wx = (warp & 1) * 4, wy = ((warp >> 1) & 1) * 4, wz = (warp >> 2) * 2;
+    const int vi = x0 + wx + (lane & 3);
+    const int vj = y0 + wy + ((lane >> 2) & 3);
+    const int vk = z0 + wz + (lane >> 4);
     const int volCenter = (int)((float)V) / 2;
     const int imgCenter = (int)((float)M) / 2;
 
@@ -257,17 +332,17 @@ bp_kernel(float *__restrict__ vol, int V, const TI *__restrict__ img, int M,
     const int convW = (int)roundf(kerHW);
     const float kerCenter = ((float)kerSize - 1) / 2;
     const float kerScale = kerCenter / kerHW;
+    const float kerCenterHalf = kerCenter + 0.5f;
     // reach of the brick / warp sub-brick along the projection direction
     const float bcx = x0 + 0.5f * (kBpBX - 1) - volCenter, bcy = y0 + 0.5f * (kBpBY - 1) - volCenter,
                 bcz = z0 + 0.5f * (kBpBZ - 1) - volCenter;
-    const int warp = tid >> 5;
-    const float wcx = bcx, wcy = y0 + (warp & 1) * 4 + 1.5f - volCenter, wcz = z0 + (warp >> 1) - volCenter;
+    const float wcx = x0 + wx + 1.5f - volCenter, wcy = y0 + wy + 1.5f - volCenter, wcz = z0 + wz + 0.5f - volCenter;
     // slab half-thickness: kerHW for the reference rule; for the adjoint, any
     // voxel within the 4^3 window of a sample point (|r| < 2 per axis)
     const float slab = ADJ ? 2.0f * 1.7320508f + kCullEps : kerHW + kCullEps;
     const int MM = M * M;
 
-    float accAll = 0.0f;
+    float accAll = 0.0f, accW = 0.0f;
     for (int c0 = 0; c0 < n; c0 += kBpChunk) {
         const int cn = min(kBpChunk, n - c0);
         __syncthreads();
@@ -304,41 +379,31 @@ bp_kernel(float *__restrict__ vol, int V, const TI *__restrict__ img, int M,
             const float nx0 = ax[0], nx1 = ax[1], nx2 = ax[2];
             const float ny0 = ax[3], ny1 = ax[4], ny2 = ax[5];
             const float nz0 = ax[6], nz1 = ax[7], nz2 = ax[8];
-            {   // warp-level cull (uniform across the warp)
+            {   // warp-level cull (uniform across the warp): the warp's 4x4x2 block
                 const float d = wcx * nz0 + wcy * nz1 + wcz * nz2;
-                const float ext = 0.5f * ((kBpBX - 1) * fabsf(nz0) + 3.0f * fabsf(nz1));
+                const float ext = 0.5f * (3.0f * fabsf(nz0) + 3.0f * fabsf(nz1) + fabsf(nz2));
                 if (fabsf(d) > slab + ext) continue;
             }
             if (!active) continue;
             const TI *img_ptr = img + (size_t)(c0 + al) * MM;
             if (!ADJ) {
                 // gpuBackProject.cu:62-107
-                const float f_imgi = ((float)vi - volCenter) * nx0 + ((float)vj - volCenter) * nx1 + ((float)vk - volCenter) * nx2 + imgCenter;
-                const float f_imgj = ((float)vi - volCenter) * ny0 + ((float)vj - volCenter) * ny1 + ((float)vk - volCenter) * ny2 + imgCenter;
-                const float f_imgk = ((float)vi - volCenter) * nz0 + ((float)vj - volCenter) * nz1 + ((float)vk - volCenter) * nz2;
+                const float a0 = (float)vi - volCenter, a1 = (float)vj - volCenter, a2 = (float)vk - volCenter;
+                const float f_imgi = __fadd_rn(voxel_proj(a0, a1, a2, nx0, nx1, nx2), (float)imgCenter);
+                const float f_imgj = __fadd_rn(voxel_proj(a0, a1, a2, ny0, ny1, ny2), (float)imgCenter);
+                const float f_imgk = voxel_proj(a0, a1, a2, nz0, nz1, nz2);
                 if (!(fabsf(f_imgk) <= kerHW)) continue;
                 const int imgi = (int)roundf(f_imgi);
                 const int imgj = (int)roundf(f_imgj);
-                float cumSum = 0.0f;
-                for (int j1 = imgj - convW; j1 <= imgj + convW; j1++) {
-                    for (int i1 = imgi - convW; i1 <= imgi + convW; i1++) {
-                        float imgi1 = (i1 - imgCenter) * nx0 + (j1 - imgCenter) * ny0 + volCenter;
-                        float r = fminf(fmaxf((float)imgi1 - vi, (float)-convW), (float)convW);
-                        int kidx = min(max(kb_index(r, kerScale, kerCenter), 0), kerSize - 1);
-                        float w = sker[kidx];
-                        float imgj1 = (i1 - imgCenter) * nx1 + (j1 - imgCenter) * ny1 + volCenter;
-                        r = fminf(fmaxf((float)imgj1 - vj, (float)-convW), (float)convW);
-                        kidx = min(max(kb_index(r, kerScale, kerCenter), 0), kerSize - 1);
-                        w = w * sker[kidx];
-                        float imgk1 = (i1 - imgCenter) * nx2 + (j1 - imgCenter) * ny2 + volCenter;
-                        r = fminf(fmaxf((float)imgk1 - vk, (float)-convW), (float)convW);
-                        kidx = min(max(kb_index(r, kerScale, kerCenter), 0), kerSize - 1);
-                        w = w * sker[kidx];
-                        const int lin = j1 * M + i1;
-                        if (lin < MM && lin >= 0) cumSum += (ONES ? 1.0f : ld_f32(img_ptr + lin)) * w;
-                    }
-                }
+                float cumSum = 0.0f, cumW = 0.0f;
+                const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk, (float)volCenter,
+                                   kerScale, kerCenter + 0.5f};
+                if (imgi >= 2 && imgj >= 2 && imgi + 2 < M && imgj + 2 < M)
+                    ref_window<TI, ONES, DENS, true>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cumSum, cumW);
+                else
+                    ref_window<TI, ONES, DENS, false>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cumSum, cumW);
                 accAll += cumSum;
+                if (DENS) accW += cumW;
             } else {
                 // Exact adjoint of fp_kernel<., 4>: every pixel whose 4^3
                 // window contains this voxel, with the forward weight.  Such a
@@ -362,9 +427,9 @@ bp_kernel(float *__restrict__ vol, int V, const TI *__restrict__ img, int M,
                         // membership in the forward window floor(f)-1 .. floor(f)+2
                         const int oi = vi - ((int)floorf(fi) - 1), oj = vj - ((int)floorf(fj) - 1), ok = vk - ((int)floorf(fk) - 1);
                         if ((unsigned)oi > 3u || (unsigned)oj > 3u || (unsigned)ok > 3u) continue;
-                        const float w = kb_weight(sker, (float)vi - fi, kerScale, kerCenter, kerSize) *
-                                        kb_weight(sker, (float)vj - fj, kerScale, kerCenter, kerSize) *
-                                        kb_weight(sker, (float)vk - fk, kerScale, kerCenter, kerSize);
+                        const float w = kb_weight(sker, (float)vi - fi, kerScale, kerCenterHalf, kerSize) *
+                                        kb_weight(sker, (float)vj - fj, kerScale, kerCenterHalf, kerSize) *
+                                        kb_weight(sker, (float)vk - fk, kerScale, kerCenterHalf, kerSize);
                         s = fmaf(w, ld_f32(img_ptr + (size_t)pxj * M + pxi), s);
                     }
                 }
@@ -373,20 +438,21 @@ bp_kernel(float *__restrict__ vol, int V, const TI *__restrict__ img, int M,
         }
     }
     if (active) {
-        float *p = vol + (size_t)vk * V * V + (size_t)vj * V + vi;
-        *p = *p + accAll * (d_scale ? *d_scale : 1.0f);
+        const size_t o = (size_t)vk * V * V + (size_t)vj * V + vi;
+        vol[o] = vol[o] + accAll * (d_scale ? *d_scale : 1.0f);
+        if (DENS) pd[o] = pd[o] + accW;
     }
 }
 
-template <typename TI, bool ONES, bool ADJ>
+template <typename TI, bool ONES, bool ADJ, bool DENS = false>
 static cudaError_t launch_bp_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
-                               const Geom &g, const float *scale, cudaStream_t s)
+                               const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr)
 {
     if (n <= 0) return cudaSuccess;
     const int bx = (g.V + kBpBX - 1) / kBpBX, by = (g.V + kBpBY - 1) / kBpBY, bz = (g.V + kBpBZ - 1) / kBpBZ;
     const long long nb = (long long)bx * by * bz;
-    bp_kernel<TI, ONES, ADJ><<<(unsigned)nb, kBpThreads, 0, s>>>(vol, g.V, img, g.M, axes, n, g.mask_radius, ker,
-                                                                 g.ker_size, g.ker_hw, bx, by, scale);
+    bp_kernel<TI, ONES, ADJ, DENS><<<(unsigned)nb, kBpThreads, 0, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius,
+                                                                       ker, g.ker_size, g.ker_hw, bx, by, scale);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -398,6 +464,17 @@ cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, 
     if (iprec == kF32) return launch_bp_t<float, false, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
     if (iprec == kF16) return launch_bp_t<__half, false, false>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
     return launch_bp_t<__nv_bfloat16, false, false>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g, scale, s);
+}
+
+cudaError_t launch_back_project_ref_density(float *d_vol, float *d_pd, const void *d_img, int iprec, const float *d_ker,
+                                            const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
+{
+    if (iprec == kF32)
+        return launch_bp_t<float, false, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
+    if (iprec == kF16)
+        return launch_bp_t<__half, false, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
+    return launch_bp_t<__nv_bfloat16, false, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g, scale,
+                                                          s, d_pd);
 }
 
 cudaError_t launch_back_project_adjoint(float *d_vol, const void *d_img, int iprec, const float *d_ker,

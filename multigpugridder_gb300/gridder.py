@@ -43,6 +43,12 @@ def _f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
 
 
+def _own(a):
+    """A private FP32 copy: the object keeps arrays by value, as MATLAB does,
+    so resetVolume() and later calls never write into the caller's arrays."""
+    return np.array(a, dtype=np.float32, order="C", copy=True)
+
+
 def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else None
 
@@ -142,7 +148,7 @@ class MultiGPUGridder:
     # ---------------------------------------------------------------- MATLAB API
     def setVolume(self, vol):
         """setVolume (MultiGPUGridder_Matlab_Class.m:272-275) + the CAS preparation."""
-        self.Volume = _f32(vol)
+        self.Volume = _own(vol)
         n = self.VolumeSize
         if self.Volume.shape != (n, n, n):
             raise ValueError("Volume must be %d^3 (got %s)" % (n, self.Volume.shape))
@@ -166,7 +172,7 @@ class MultiGPUGridder:
         if len(args) == 1:
             axes = self._axes(args[0])
         elif len(args) == 3:
-            self.Volume = _f32(args[0])
+            self.Volume = _own(args[0])
             axes = self._axes(args[1])
             self.setMaskRadius(args[2])
             self._cas_from_volume = False
@@ -193,7 +199,7 @@ class MultiGPUGridder:
         (gpuGridder.cpp:330-332)."""
         ax = self._axes(axes if axes is not None else self.coordAxes)
         if images is not None:
-            self.Images = _f32(images)
+            self.Images = _own(images)
             self.coordAxes = ax
             self._call("gg_back_project", _ptr(ax), ax.shape[0], _ptr(self.Images), None, 0)
         elif not self.RunFFTOnGPU and self.CASImages is not None:
@@ -245,7 +251,7 @@ class MultiGPUGridder:
         """reconstructVol (MultiGPUGridder_Matlab_Class.m:284-312): back projection
         divided by the plane density (+1e-6), then getVol."""
         if images is not None:
-            self.Images = _f32(images)
+            self.Images = _own(images)
             self.coordAxes = self._axes(axes)
         ax = self._axes(self.coordAxes)
         n = self.VolumeSize

@@ -11,9 +11,14 @@
  *   - gpuBackProjectKernel      src/Projection/gpuBackProject.cu:4-113
  * in three forms:
  *   *_ref_f32   single precision, same operation order, roundf() index
- *               rounding, int mask radius, linear-index bounds checks.
- *               Compiled with -ffp-contract=off so that it gives the same
- *               bits on x86-64 and aarch64.
+ *               rounding, int mask radius, linear-index bounds checks, and
+ *               the fused multiply-adds the reference's nvcc build forms:
+ *               table index roundf(fma(r, kerScale, kerCenter)), sums
+ *               acc = fma(x, w, acc), sample coordinates fma(a, x, b*y) + c.
+ *               (Identified by replaying the reference kernels' own outputs,
+ *               tests/golden/reference_kernels.npz, bit for bit.)  Compiled
+ *               with -ffp-contract=off and explicit fmaf(), so it gives the
+ *               same bits on x86-64 and aarch64.
  *   *_f64       the same discrete operator evaluated in double precision
  *               (same float KB table, same nearest-index rule), the
  *               "FP64 oracle" the reduced-precision forms are measured against.
@@ -84,22 +89,23 @@ void gg_oracle_fp_ref_f32(const float *vol, int V, float *img, int M,
                 float r = sqrtf((float)(i - imgCenter) * (i - imgCenter) +
                                 (float)((j - imgCenter) * (j - imgCenter)));
                 if (!(r <= maskR)) continue;
-                float fi = nx[0] * ((float)(i - imgCenter)) + ny[0] * ((float)(j - imgCenter)) + (float)volCenter;
-                float fj = nx[1] * ((float)(i - imgCenter)) + ny[1] * ((float)(j - imgCenter)) + (float)volCenter;
-                float fk = nx[2] * ((float)(i - imgCenter)) + ny[2] * ((float)(j - imgCenter)) + (float)volCenter;
+                const float x = (float)(i - imgCenter), y = (float)(j - imgCenter);
+                float fi = fmaf(nx[0], x, ny[0] * y) + (float)volCenter;
+                float fj = fmaf(nx[1], x, ny[1] * y) + (float)volCenter;
+                float fk = fmaf(nx[2], x, ny[2] * y) + (float)volCenter;
                 int ii = (int)roundf(fi), jj = (int)roundf(fj), kk = (int)roundf(fk);
                 float acc = 0.0f;
                 for (int i1 = ii - convW; i1 <= ii + convW; i1++) {
                     float ri = fclampf((float)i1 - fi, (float)-convW, (float)convW);
-                    int ki = imin(imax((int)roundf(ri * kerScale + kerCenter), 0), ker_size - 1);
+                    int ki = imin(imax((int)roundf(fmaf(ri, kerScale, kerCenter)), 0), ker_size - 1);
                     float wi = ker[ki];
                     for (int j1 = jj - convW; j1 <= jj + convW; j1++) {
                         float rj = fclampf((float)j1 - fj, (float)-convW, (float)convW);
-                        int kj = imin(imax((int)roundf(rj * kerScale + kerCenter), 0), ker_size - 1);
+                        int kj = imin(imax((int)roundf(fmaf(rj, kerScale, kerCenter)), 0), ker_size - 1);
                         float wj = ker[kj];
                         for (int k1 = kk - convW; k1 <= kk + convW; k1++) {
                             float rk = fclampf((float)k1 - fk, (float)-convW, (float)convW);
-                            int kx = imin(imax((int)roundf(rk * kerScale + kerCenter), 0), ker_size - 1);
+                            int kx = imin(imax((int)roundf(fmaf(rk, kerScale, kerCenter)), 0), ker_size - 1);
                             float wk = ker[kx];
                             float w = wi * wj * wk;
                             long long lin = (long long)k1 * V * V + (long long)j1 * V + i1;
@@ -107,7 +113,7 @@ void gg_oracle_fp_ref_f32(const float *vol, int V, float *img, int M,
                                lower-bound check is added so a bad input cannot
                                read outside the buffer here */
                             if (lin < V3 && lin >= 0)
-                                acc = acc + w * vol[lin];
+                                acc = fmaf(w, vol[lin], acc);
                         }
                     }
                 }
@@ -201,9 +207,10 @@ void gg_oracle_bp_ref_f32(float *vol, int V, const float *img, int M,
                     const float *nx = axes + 9 * (size_t)a;
                     const float *ny = nx + 3;
                     const float *nz = ny + 3;
-                    float f_imgi = ((float)vi - volCenter) * nx[0] + ((float)vj - volCenter) * nx[1] + ((float)vk - volCenter) * nx[2] + imgCenter;
-                    float f_imgj = ((float)vi - volCenter) * ny[0] + ((float)vj - volCenter) * ny[1] + ((float)vk - volCenter) * ny[2] + imgCenter;
-                    float f_imgk = ((float)vi - volCenter) * nz[0] + ((float)vj - volCenter) * nz[1] + ((float)vk - volCenter) * nz[2];
+                    const float a0 = (float)vi - volCenter, a1 = (float)vj - volCenter, a2 = (float)vk - volCenter;
+                    float f_imgi = fmaf(a2, nx[2], fmaf(a0, nx[0], a1 * nx[1])) + imgCenter;
+                    float f_imgj = fmaf(a2, ny[2], fmaf(a0, ny[0], a1 * ny[1])) + imgCenter;
+                    float f_imgk = fmaf(a2, nz[2], fmaf(a0, nz[0], a1 * nz[1]));
                     if (!(fabsf(f_imgk) <= ker_hw)) continue;
                     int imgi = (int)roundf(f_imgi);
                     int imgj = (int)roundf(f_imgj);
@@ -211,24 +218,25 @@ void gg_oracle_bp_ref_f32(float *vol, int V, const float *img, int M,
                     float cumSum = 0;
                     for (int j1 = imgj - convW; j1 <= imgj + convW; j1++) {
                         for (int i1 = imgi - convW; i1 <= imgi + convW; i1++) {
-                            float p = (i1 - imgCenter) * nx[0] + (j1 - imgCenter) * ny[0] + volCenter;
+                            const float pi = (float)(i1 - imgCenter), pj = (float)(j1 - imgCenter);
+                            float p = fmaf(pi, nx[0], pj * ny[0]) + volCenter;
                             float rr = fclampf(p - vi, (float)-convW, (float)convW);
-                            int kidx = imin(imax((int)roundf(rr * kerScale + kerCenter), 0), ker_size - 1);
+                            int kidx = imin(imax((int)roundf(fmaf(rr, kerScale, kerCenter)), 0), ker_size - 1);
                             float w = ker[kidx];
-                            p = (i1 - imgCenter) * nx[1] + (j1 - imgCenter) * ny[1] + volCenter;
+                            p = fmaf(pi, nx[1], pj * ny[1]) + volCenter;
                             rr = fclampf(p - vj, (float)-convW, (float)convW);
-                            kidx = imin(imax((int)roundf(rr * kerScale + kerCenter), 0), ker_size - 1);
+                            kidx = imin(imax((int)roundf(fmaf(rr, kerScale, kerCenter)), 0), ker_size - 1);
                             w = w * ker[kidx];
-                            p = (i1 - imgCenter) * nx[2] + (j1 - imgCenter) * ny[2] + volCenter;
+                            p = fmaf(pi, nx[2], pj * ny[2]) + volCenter;
                             rr = fclampf(p - vk, (float)-convW, (float)convW);
-                            kidx = imin(imax((int)roundf(rr * kerScale + kerCenter), 0), ker_size - 1);
+                            kidx = imin(imax((int)roundf(fmaf(rr, kerScale, kerCenter)), 0), ker_size - 1);
                             w = w * ker[kidx];
                             long long lin = (long long)j1 * M + i1;
                             /* linear-index check only: windows that cross a
                                row edge wrap into the neighbouring row, as in
                                gpuBackProject.cu:99 */
                             if (lin < (long long)M * M && lin >= 0)
-                                cumSum += img_ptr[lin] * w;
+                                cumSum = fmaf(img_ptr[lin], w, cumSum);
                         }
                     }
                     cumSumAllAxes += cumSum;
