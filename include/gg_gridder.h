@@ -137,6 +137,16 @@ int gg_get_volume_dev(gg_gridder *h, float *d_volume_out, void *stream);
 int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int n_axes,
                               const float *d_images, float *d_volume_out, void *stream);
 
+/* Exact adjoint of the whole forward operator (setVolume's CAS preparation
+   followed by forwardProject to images): image gradients n*N*N -> volume
+   gradient N^3 (written, not accumulated).  Uses the exact-adjoint back
+   projection whatever gg_set_bp_mode says and leaves the resident CAS volume
+   untouched.  No counterpart in the reference, which has no gradient. */
+int gg_forward_project_adjoint(gg_gridder *h, const float *axes, int n_axes, const float *image_grads,
+                               float *volume_grad_out);
+int gg_forward_project_adjoint_dev(gg_gridder *h, const float *d_axes, int n_axes, const float *d_image_grads,
+                                   float *d_volume_grad_out, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Stateless kernel entry points (device pointers).
  * ------------------------------------------------------------------------- */

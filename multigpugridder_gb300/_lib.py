@@ -66,6 +66,8 @@ SIGNATURES = {
     "gg_back_project_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _c_int, _vp]),
     "gg_get_volume_dev": (_c_int, [_vp, _fp, _vp]),
     "gg_reconstruct_volume_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _vp]),
+    "gg_forward_project_adjoint": (_c_int, [_vp, _fp, _c_int, _fp, _fp]),
+    "gg_forward_project_adjoint_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _vp]),
     "gg_forward_project_kernel": (_c_int, [_fp, _fp, _fp, _fp, _c_float, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _vp]),
     "gg_back_project_kernel": (_c_int, [_fp, _fp, _fp, _fp, _c_float, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _vp]),
     "gg_back_project_adjoint_kernel": (_c_int, [_fp, _fp, _fp, _fp, _c_float, _c_int, _c_int, _c_int, _c_int, _c_int, _vp]),

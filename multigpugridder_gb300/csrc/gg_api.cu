@@ -74,6 +74,10 @@ struct GGError {
 template <typename T> struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
     void ensure(size_t count)
     {
         if (count <= n && p) return;
@@ -147,6 +151,7 @@ struct gg_gridder {
     DevBuf<uint16_t> cas_lp; // FP16/BF16 copy read by the forward projection
     bool cas_lp_valid = false;
     DevBuf<float> pd;        // plane density V^3
+    DevBuf<float> adj;       // CAS-volume gradient V^3 (forward-operator adjoint)
     DevBuf<float> axes;
     DevBuf<float> vol_io;    // N^3
     DevBuf<float> x3;        // M^3 real FFT input/output
@@ -406,6 +411,38 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
     }
 }
 
+// Exact adjoint of (CAS preparation + forward projection + CAS images ->
+// images): image gradients (device, n*N*N) -> volume gradient (device, N^3).
+void forward_adjoint(gg_gridder *h, const float *d_axes, int n, const float *d_img_grad, float *d_vol_grad, cudaStream_t s)
+{
+    const size_t V3 = (size_t)h->V * h->V * h->V, NN = (size_t)h->N * h->N;
+    h->adj.ensure(V3);
+    GG_CK(cudaMemsetAsync(h->adj.p, 0, V3 * sizeof(float), s));
+    const int B = h->max_batch;
+    for (int a0 = 0; a0 < n; a0 += B) {
+        const int b = std::min(B, n - a0);
+        ensure_slot(h, 0, B, false);
+        auto &S = h->slot[0];
+        GG_CK(launch_images_to_fft_input(d_img_grad + (size_t)a0 * NN, h->N, h->M, b, S.real.p, s));
+        cufftHandle p = plan2d(h, CUFFT_R2C, b);
+        GG_CKF(cufftSetStream(p, s));
+        GG_CKF(cufftExecR2C(p, S.real.p, S.spec.p));
+        GG_CK(launch_spectrum_to_cas_images_adjoint(S.spec.p, h->M, b, S.casimg.p, s));
+        ProfScope ps(h, s, GG_KERNEL_BACK);
+        GG_CK(launch_back_project_adjoint(h->adj.p, S.casimg.p, kF32, h->ker.p, d_axes + (size_t)a0 * 9, b, h->geom(),
+                                          nullptr, s));
+        ps.done();
+    }
+    const size_t M3 = (size_t)h->M * h->M * h->M;
+    h->x3.ensure(M3);
+    h->spec3.ensure((size_t)h->M * h->M * (h->M / 2 + 1));
+    GG_CK(launch_cas_volume_adjoint_input(h->adj.p, h->V, h->M, h->x3.p, s));
+    cufftHandle p = plan3(h, true);
+    GG_CKF(cufftSetStream(p, s));
+    GG_CKF(cufftExecR2C(p, h->x3.p, h->spec3.p));
+    GG_CK(launch_spectrum_to_vol_adjoint(h->spec3.p, h->M, h->N, h->precomp.p, d_vol_grad, s));
+}
+
 void upload_axes(gg_gridder *h, const float *axes, int n, cudaStream_t s)
 {
     h->axes.ensure((size_t)(n > 0 ? n : 1) * 9);
@@ -562,6 +599,7 @@ void destroy_handle(gg_gridder *h)
     h->cas.release();
     h->cas_lp.release();
     h->pd.release();
+    h->adj.release();
     h->axes.release();
     h->vol_io.release();
     h->x3.release();
@@ -1012,6 +1050,43 @@ extern "C" int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int
         do_get_volume(h, h->cas.p, d_volume_out, s);
         h->cas_lp_valid = false;
         end_dev(h, s);
+    });
+}
+
+extern "C" int gg_forward_project_adjoint_dev(gg_gridder *h, const float *d_axes, int n_axes, const float *d_image_grads,
+                                              float *d_volume_grad_out, void *stream)
+{
+    return guarded(h, [&] {
+        check_axes_count(n_axes);
+        if (n_axes > 0 && (!d_axes || !d_image_grads)) fail(GG_ERR_INVALID_ARG, "axes and image gradients are required");
+        if (!d_volume_grad_out) fail(GG_ERR_INVALID_ARG, "output is NULL");
+        if (h->five_taps) fail(GG_ERR_STATE, "the adjoint needs a KB table with zero edge values");
+        cudaStream_t s = (cudaStream_t)stream;
+        begin_dev(h, s);
+        forward_adjoint(h, d_axes, n_axes, d_image_grads, d_volume_grad_out, s);
+        end_dev(h, s);
+    });
+}
+
+extern "C" int gg_forward_project_adjoint(gg_gridder *h, const float *axes, int n_axes, const float *image_grads,
+                                          float *volume_grad_out)
+{
+    return guarded(h, [&] {
+        check_axes_count(n_axes);
+        if (n_axes > 0 && (!axes || !image_grads)) fail(GG_ERR_INVALID_ARG, "axes and image gradients are required");
+        if (!volume_grad_out) fail(GG_ERR_INVALID_ARG, "output is NULL");
+        if (h->five_taps) fail(GG_ERR_STATE, "the adjoint needs a KB table with zero edge values");
+        const size_t NN = (size_t)h->N * h->N, N3 = NN * h->N;
+        upload_axes(h, axes, n_axes, h->cs);
+        DevBuf<float> g;
+        g.ensure(std::max<size_t>(1, NN * (size_t)n_axes));
+        if (n_axes > 0)
+            GG_CK(cudaMemcpyAsync(g.p, image_grads, NN * (size_t)n_axes * sizeof(float), cudaMemcpyHostToDevice, h->cs));
+        h->vol_io.ensure(N3);
+        forward_adjoint(h, h->axes.p, n_axes, g.p, h->vol_io.p, h->cs);
+        GG_CK(cudaMemcpyAsync(volume_grad_out, h->vol_io.p, N3 * sizeof(float), cudaMemcpyDeviceToHost, h->cs));
+        GG_CK(cudaStreamSynchronize(h->cs));
+        g.release();
     });
 }
 

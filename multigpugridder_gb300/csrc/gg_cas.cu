@@ -203,6 +203,78 @@ __global__ void spectrum_to_cas_images_kernel(const cufftComplex *__restrict__ s
     }
 }
 
+// ---- adjoint of the whole forward operator ----------------------------------
+// Gradient of images -> CAS images: the adjoint of (FromCAS, shift, inverse
+// FFT / M^2, shift, real part, crop).  For the FFT of a real image FromCAS^T
+// equals Re+Im, so this is spectrum_to_cas_images with the first row and
+// column (zeroed by FromCAS) dropped and the 1/M^2 applied.
+__global__ void spectrum_to_cas_images_adjoint_kernel(const cufftComplex *__restrict__ spec, int M, int n,
+                                                      float *__restrict__ cas)
+{
+    const int H = M / 2 + 1;
+    const size_t per = (size_t)M * M;
+    const size_t total = per * n;
+    const float scale = 1.0f / ((float)M * (float)M);
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t a = e / per;
+        const int rem = (int)(e - a * per);
+        const int i = rem % M, j = rem / M;
+        float out = 0.0f;
+        if (i != 0 && j != 0) {
+            const int u = shift_idx(i, M), v = shift_idx(j, M);
+            const cufftComplex *s = spec + a * (size_t)M * H;
+            if (u <= M / 2) {
+                const cufftComplex c = s[(size_t)v * H + u];
+                out = c.x + c.y;
+            } else {
+                const int v2 = v ? M - v : 0;
+                const cufftComplex c = s[(size_t)v2 * H + (M - u)];
+                out = c.x - c.y;
+            }
+        }
+        cas[e] = out * scale;
+    }
+}
+
+// Gradient of the CAS volume -> volume, first half: crop V^3 to the inner M^3
+// and fftshift (the adjoint of the zero-pad and of the output fftshift).
+__global__ void cas_volume_adjoint_input_kernel(const float *__restrict__ g, int V, int M, float *__restrict__ x)
+{
+    const size_t total = (size_t)M * M * M;
+    const int b = V / 2 - M / 2;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int qi = (int)(e % M), qj = (int)((e / M) % M), qk = (int)(e / ((size_t)M * M));
+        const int i = shift_idx(qi, M), j = shift_idx(qj, M), k = shift_idx(qk, M);
+        x[e] = g[((size_t)(k + b) * V + (j + b)) * V + (i + b)];
+    }
+}
+
+// Second half: Re+Im of fftshift(FFT), times the precomp, centred crop to N^3.
+// (The adjoint of ToCAS maps g to g + i g; with the unnormalised FFT's adjoint
+// M^3 * ifft of a real input equal to conj(fft), Re((1+i) conj(F)) = Re F + Im F.)
+__global__ void spectrum_to_vol_adjoint_kernel(const cufftComplex *__restrict__ spec, int M, int N,
+                                               const double *__restrict__ pc, float *__restrict__ vol)
+{
+    const size_t total = (size_t)N * N * N;
+    const int ob = M / 2 - N / 2;
+    const int H = M / 2 + 1;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int oi = (int)(e % N), oj = (int)((e / N) % N), ok = (int)(e / ((size_t)N * N));
+        const int i = oi + ob, j = oj + ob, k = ok + ob;
+        const int u = shift_idx(i, M), v = shift_idx(j, M), w = shift_idx(k, M);
+        float val;
+        if (u <= M / 2) {
+            const cufftComplex c = spec[((size_t)w * M + v) * H + u];
+            val = c.x + c.y;
+        } else {
+            const int w2 = w ? M - w : 0, v2 = v ? M - v : 0;
+            const cufftComplex c = spec[((size_t)w2 * M + v2) * H + (M - u)];
+            val = c.x - c.y;
+        }
+        vol[e] = (float)((double)val * pc[i] * pc[j] * pc[k]);
+    }
+}
+
 __global__ void divide_plane_density_kernel(float *__restrict__ a, const float *__restrict__ b, size_t count, float eps)
 {
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < count; e += (size_t)gridDim.x * blockDim.x)
@@ -305,6 +377,29 @@ cudaError_t launch_spectrum_to_cas_images(const cufftComplex *d_spec, int M, int
     if (prec == kF32) spectrum_to_cas_images_kernel<float><<<g, kT, 0, s>>>(d_spec, M, n, (float *)d_cas, d_scale);
     else if (prec == kF16) spectrum_to_cas_images_kernel<__half><<<g, kT, 0, s>>>(d_spec, M, n, (__half *)d_cas, d_scale);
     else spectrum_to_cas_images_kernel<__nv_bfloat16><<<g, kT, 0, s>>>(d_spec, M, n, (__nv_bfloat16 *)d_cas, d_scale);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectrum_to_cas_images_adjoint(const cufftComplex *d_spec, int M, int n, float *d_cas, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    spectrum_to_cas_images_adjoint_kernel<<<grid_for((size_t)M * M * n, kT), kT, 0, s>>>(d_spec, M, n, d_cas);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cas_volume_adjoint_input(const float *d_g, int V, int M, float *d_x, cudaStream_t s)
+{
+    cas_volume_adjoint_input_kernel<<<grid_for((size_t)M * M * M, kT), kT, 0, s>>>(d_g, V, M, d_x);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectrum_to_vol_adjoint(const cufftComplex *d_spec, int M, int N, const double *d_precomp, float *d_vol,
+                                           cudaStream_t s)
+{
+    spectrum_to_vol_adjoint_kernel<<<grid_for((size_t)N * N * N, kT), kT, 0, s>>>(d_spec, M, N, d_precomp, d_vol);
     count_launches(1);
     return cudaGetLastError();
 }

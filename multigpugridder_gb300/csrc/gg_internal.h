@@ -81,6 +81,16 @@ cudaError_t launch_images_to_fft_input(const float *d_img, int N, int M, int n, 
 // R2C half spectra n*M*(M/2+1) -> CAS images n*M*M (shift, Re+Im) in storage `prec`.
 cudaError_t launch_spectrum_to_cas_images(const cufftComplex *d_spec, int M, int n, void *d_cas,
                                           int prec, const float *d_scale, cudaStream_t s);
+// Adjoint of the whole forward operator (volume -> images), by stage:
+// R2C half spectra of padded, shifted image gradients -> CAS-image gradients
+// (Re+Im, first row/column zero, 1/M^2).
+cudaError_t launch_spectrum_to_cas_images_adjoint(const cufftComplex *d_spec, int M, int n, float *d_cas,
+                                                  cudaStream_t s);
+// CAS-volume gradient V^3 -> R2C input M^3 (inner crop + shift).
+cudaError_t launch_cas_volume_adjoint_input(const float *d_g, int V, int M, float *d_x, cudaStream_t s);
+// R2C spectrum -> volume gradient N^3 (Re+Im, shift, precomp, crop).
+cudaError_t launch_spectrum_to_vol_adjoint(const cufftComplex *d_spec, int M, int N, const double *d_precomp,
+                                           float *d_vol, cudaStream_t s);
 // d[0..count) = value.
 cudaError_t launch_fill(float *d, size_t count, float value, cudaStream_t s);
 // a = a / (b + eps) over `count` elements (reconstructVol's plane-density division).

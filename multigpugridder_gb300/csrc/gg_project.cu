@@ -444,6 +444,206 @@ bp_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__re
     }
 }
 
+// ---------------------------------------------------------------------------
+// Back projection, reference window rule, with in-order lane compaction
+// ---------------------------------------------------------------------------
+// Only the voxels inside a direction's slab (|f_imgk| <= 2, a few percent of
+// the volume) run the 25-pixel window, so a warp that owns one voxel per lane
+// idles about half its lanes.  Here each warp owns 128 voxels (an 8x4x4 block,
+// 4 per lane: slot s = z offset).  Per direction it tests all 128, and the
+// k-th active voxel (slot-major, lane order) is computed by lane k % 32 in
+// round k / 32; each owner lane then takes its voxel's window sum back with a
+// shuffle.  Every voxel still receives its directions one by one in order, so
+// the per-voxel sums are those of the uncompacted kernel, bit for bit.
+constexpr int kCBX = 16, kCBY = 8, kCBZ = 8; // brick: 8 warp blocks of 8x4x4
+constexpr int kCThreads = 256;
+
+__device__ __forceinline__ int nth_set_bit(unsigned m, int n)
+{
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const unsigned lo = m & ((1u << w) - 1u);
+        const int c = __popc(lo);
+        if (n >= c) {
+            n -= c;
+            m >>= w;
+            pos += w;
+        } else {
+            m = lo;
+        }
+    }
+    return pos;
+}
+
+template <typename TI, bool ONES, bool DENS>
+__global__ void __launch_bounds__(kCThreads)
+bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
+                      const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
+                      float kerHW, int bricksX, int bricksY, const float *__restrict__ d_scale)
+{
+    __shared__ float sker[kMaxKerSize];
+    __shared__ float sax[kBpChunk * 9];
+    __shared__ int slist[kBpChunk];
+    __shared__ int swarp[kBpChunk / 32];
+    __shared__ int scount;
+    // per-voxel sums [warp][slot][lane]; a voxel is updated by at most one lane
+    // per direction, directions in order, so no atomics are needed
+    __shared__ float sacc[kCThreads * 4];
+    __shared__ float saccw[DENS ? kCThreads * 4 : 1];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int x0 = (blockIdx.x % bricksX) * kCBX;
+    const int y0 = ((blockIdx.x / bricksX) % bricksY) * kCBY;
+    const int z0 = (blockIdx.x / (bricksX * bricksY)) * kCBZ;
+    const int bx = x0 + (warp & 1) * 8, by = y0 + ((warp >> 1) & 1) * 4, bz = z0 + (warp >> 2) * 4;
+    const int volCenter = (int)((float)V) / 2;
+    const int imgCenter = (int)((float)M) / 2;
+
+    {   // skip bricks entirely outside the mask sphere
+        const float cx = fmaxf(fabsf(x0 + 0.5f * (kCBX - 1) - volCenter) - 0.5f * (kCBX - 1), 0.f);
+        const float cy = fmaxf(fabsf(y0 + 0.5f * (kCBY - 1) - volCenter) - 0.5f * (kCBY - 1), 0.f);
+        const float cz = fmaxf(fabsf(z0 + 0.5f * (kCBZ - 1) - volCenter) - 0.5f * (kCBZ - 1), 0.f);
+        if (cx * cx + cy * cy + cz * cz > (float)maskR * (float)maskR + 1.0f) return;
+    }
+    load_table(sker, ker, kerSize);
+
+    const int lx = bx + (lane & 7), ly = by + (lane >> 3);
+    const long long R2 = (long long)maskR * maskR;
+    unsigned inmask = 0;
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        const int lz = bz + s;
+        const long long d2 = (long long)(lx - volCenter) * (lx - volCenter) + (long long)(ly - volCenter) * (ly - volCenter) +
+                             (long long)(lz - volCenter) * (lz - volCenter);
+        if (lx < V && ly < V && lz < V && d2 <= R2) inmask |= 1u << s;
+    }
+    const float kerCenter = ((float)kerSize - 1) / 2;
+    const float kerScale = kerCenter / kerHW;
+    const float ax0 = (float)lx - volCenter, ay0 = (float)ly - volCenter;
+    const float wcx = bx + 3.5f - volCenter, wcy = by + 1.5f - volCenter, wcz = bz + 1.5f - volCenter;
+    const float slab = kerHW + kCullEps;
+    const int MM = M * M;
+
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        sacc[(warp * 4 + s) * 32 + lane] = 0.0f;
+        if (DENS) saccw[(warp * 4 + s) * 32 + lane] = 0.0f;
+    }
+    float *wacc = sacc + warp * 128;
+    float *waccw = saccw + (DENS ? warp * 128 : 0);
+    // Directions are staged through shared memory in chunks, culled against
+    // the brick (compacted in order), then against each warp's 8x4x4 block.
+    const float bcx = x0 + 0.5f * (kCBX - 1) - volCenter, bcy = y0 + 0.5f * (kCBY - 1) - volCenter,
+                bcz = z0 + 0.5f * (kCBZ - 1) - volCenter;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (int c0 = 0; c0 < n; c0 += kBpChunk) {
+        const int cn = min(kBpChunk, n - c0);
+        __syncthreads();
+        for (int t = tid; t < cn * 9; t += kCThreads) sax[t] = __ldg(axes + (size_t)c0 * 9 + t);
+        __syncthreads();
+        bool keep = false;
+        if (tid < cn) {
+            const float *ax = sax + tid * 9;
+            const float zx = ax[6], zy = ax[7], zz = ax[8];
+            const float d = bcx * zx + bcy * zy + bcz * zz;
+            const float ext = 0.5f * ((kCBX - 1) * fabsf(zx) + (kCBY - 1) * fabsf(zy) + (kCBZ - 1) * fabsf(zz));
+            keep = fabsf(d) <= slab + ext;
+        }
+        const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) swarp[warp] = __popc(ballot);
+        __syncthreads();
+        {
+            int off = 0;
+            for (int w = 0; w < warp; w++) off += swarp[w];
+            if (keep) slist[off + __popc(ballot & lt_mask)] = tid;
+            if (tid == kCThreads - 1) {
+                int tot = 0;
+                for (int w = 0; w < kCThreads / 32; w++) tot += swarp[w];
+                scount = tot;
+            }
+        }
+        __syncthreads();
+        const int count = scount;
+
+        for (int q = 0; q < count; q++) {
+            const int al = slist[q];
+            const float *ax = sax + al * 9;
+            const float nz0 = ax[6], nz1 = ax[7], nz2 = ax[8];
+            {   // the warp's 8x4x4 block against the slab (uniform)
+                const float d = wcx * nz0 + wcy * nz1 + wcz * nz2;
+                const float ext = 0.5f * (7.0f * fabsf(nz0) + 3.0f * fabsf(nz1) + 3.0f * fabsf(nz2));
+                if (fabsf(d) > slab + ext) continue;
+            }
+            // the reference's per-voxel slab test (gpuBackProject.cu:64-66) for the 4 slots
+            unsigned b[4];
+#pragma unroll
+            for (int s = 0; s < 4; s++) {
+                const float a2 = (float)(bz + s) - volCenter;
+                const float fk = voxel_proj(ax0, ay0, a2, nz0, nz1, nz2);
+                b[s] = __ballot_sync(0xffffffffu, ((inmask >> s) & 1u) && fabsf(fk) <= kerHW);
+            }
+            const int p1 = __popc(b[0]), p2 = p1 + __popc(b[1]), p3 = p2 + __popc(b[2]);
+            const int total = p3 + __popc(b[3]);
+            if (total == 0) continue;
+            const float nx0 = ax[0], nx1 = ax[1], nx2 = ax[2];
+            const float ny0 = ax[3], ny1 = ax[4], ny2 = ax[5];
+            const TI *img_ptr = img + (size_t)(c0 + al) * MM;
+            for (int base = 0; base < total; base += 32) {
+                const int t = base + lane;
+                if (t < total) {
+                    float cs = 0.0f, cw = 0.0f;
+                    int s, l;
+                    if (t < p1) { s = 0; l = nth_set_bit(b[0], t); }
+                    else if (t < p2) { s = 1; l = nth_set_bit(b[1], t - p1); }
+                    else if (t < p3) { s = 2; l = nth_set_bit(b[2], t - p2); }
+                    else { s = 3; l = nth_set_bit(b[3], t - p3); }
+                    const int vi = bx + (l & 7), vj = by + (l >> 3), vk = bz + s;
+                    const float a0 = (float)vi - volCenter, a1 = (float)vj - volCenter, a2 = (float)vk - volCenter;
+                    const float f_imgi = __fadd_rn(voxel_proj(a0, a1, a2, nx0, nx1, nx2), (float)imgCenter);
+                    const float f_imgj = __fadd_rn(voxel_proj(a0, a1, a2, ny0, ny1, ny2), (float)imgCenter);
+                    const int imgi = (int)roundf(f_imgi);
+                    const int imgj = (int)roundf(f_imgj);
+                    const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk, (float)volCenter,
+                                       kerScale, kerCenter + 0.5f};
+                    if (imgi >= 2 && imgj >= 2 && imgi + 2 < M && imgj + 2 < M)
+                        ref_window<TI, ONES, DENS, true>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cs, cw);
+                    else
+                        ref_window<TI, ONES, DENS, false>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cs, cw);
+                    // cumSumAllAxes += cumSum (gpuBackProject.cu:106), in direction order
+                    const int slot = s * 32 + l;
+                    wacc[slot] = __fadd_rn(wacc[slot], cs);
+                    if (DENS) waccw[slot] = __fadd_rn(waccw[slot], cw);
+                }
+            }
+            __syncwarp();  // the next direction may update these slots from other lanes
+        }
+    }
+    __syncwarp();
+    const float sc = d_scale ? *d_scale : 1.0f;
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        if (!((inmask >> s) & 1u)) continue;
+        const size_t o = (size_t)(bz + s) * V * V + (size_t)ly * V + lx;
+        vol[o] = vol[o] + wacc[s * 32 + lane] * sc;
+        if (DENS) pd[o] = pd[o] + waccw[s * 32 + lane];
+    }
+}
+
+template <typename TI, bool ONES, bool DENS = false>
+static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
+                                       const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr)
+{
+    if (n <= 0) return cudaSuccess;
+    const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
+    const long long nb = (long long)bx * by * bz;
+    bp_ref_compact_kernel<TI, ONES, DENS><<<(unsigned)nb, kCThreads, 0, s>>>(vol, pd, g.V, img, g.M, axes, n,
+                                                                             g.mask_radius, ker, g.ker_size, g.ker_hw,
+                                                                             bx, by, scale);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
 template <typename TI, bool ONES, bool ADJ, bool DENS = false>
 static cudaError_t launch_bp_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
                                const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr)
@@ -460,21 +660,21 @@ static cudaError_t launch_bp_t(float *vol, const TI *img, const float *ker, cons
 cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, bool ones, const float *d_ker,
                                     const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
 {
-    if (ones) return launch_bp_t<float, true, false>(d_vol, nullptr, d_ker, d_axes, n, g, scale, s);
-    if (iprec == kF32) return launch_bp_t<float, false, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
-    if (iprec == kF16) return launch_bp_t<__half, false, false>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
-    return launch_bp_t<__nv_bfloat16, false, false>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g, scale, s);
+    if (ones) return launch_bp_compact_t<float, true>(d_vol, nullptr, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF32) return launch_bp_compact_t<float, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF16) return launch_bp_compact_t<__half, false>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
+    return launch_bp_compact_t<__nv_bfloat16, false>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g, scale, s);
 }
 
 cudaError_t launch_back_project_ref_density(float *d_vol, float *d_pd, const void *d_img, int iprec, const float *d_ker,
                                             const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
 {
     if (iprec == kF32)
-        return launch_bp_t<float, false, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
+        return launch_bp_compact_t<float, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
     if (iprec == kF16)
-        return launch_bp_t<__half, false, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
-    return launch_bp_t<__nv_bfloat16, false, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g, scale,
-                                                          s, d_pd);
+        return launch_bp_compact_t<__half, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
+    return launch_bp_compact_t<__nv_bfloat16, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g,
+                                                           scale, s, d_pd);
 }
 
 cudaError_t launch_back_project_adjoint(float *d_vol, const void *d_img, int iprec, const float *d_ker,

@@ -403,6 +403,33 @@ def reconstruct_vol(imgs, axes, p, precision="f64"):
     return vol_from_cas(cas / (pd + 1e-6), p.N, p.hw, p.interp), cas, pd
 
 
+def forward_operator(vol, axes, p):
+    """The whole forward operator in FP64, volume -> images (linear in vol)."""
+    return forward_project(vol, axes, p, "f64")[0]
+
+
+def forward_adjoint(y, axes, p):
+    """Exact adjoint of forward_operator, images -> volume, in FP64 (no
+    reference counterpart).  By stage:
+      images -> CAS images: pad, shift, FFT, shift, Re+Im (FromCAS^T of a
+        Hermitian spectrum), first row and column zeroed, / M^2;
+      CAS images -> CAS volume: bp_adjoint_f64;
+      CAS volume -> volume: inner crop, shift, FFT, shift, Re+Im, * precomp,
+        centred crop (ToCAS^T maps g to (1+i) g and the unnormalised FFT's
+        adjoint of a real input is conj(FFT), so Re((1+i) conj(F)) = Re F + Im F)."""
+    M, N = p.M, p.N
+    ci = cas_imgs_from_imgs(y, M)
+    ci[:, 0, :] = 0
+    ci[:, :, 0] = 0
+    ci /= float(M) * M
+    G = bp_adjoint_f64(ci, axes, p.V, p.mask_radius, p.ker, p.hw)
+    b = p.V // 2 - M // 2
+    F = np.fft.fftshift(np.fft.fftn(np.fft.fftshift(G[b:b + M, b:b + M, b:b + M])))
+    R = to_cas(F) * _precomp3(M, p.hw)
+    ob = M // 2 - N // 2
+    return R[ob:ob + N, ob:ob + N, ob:ob + N]
+
+
 # --------------------------------------------------------------------------
 # Fixture generators
 # --------------------------------------------------------------------------

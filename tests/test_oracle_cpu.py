@@ -278,6 +278,20 @@ def test_adjoint_exact_and_reference_rule_not():
     assert abs(lhs - np.sum(x * O.bp_ref_f64(y, axes, p.V, p.mask_radius, p.ker))) > 1e-3 * abs(lhs)
 
 
+def test_whole_operator_adjoint():
+    """forward_adjoint is the exact adjoint of volume -> images (CAS prep,
+    forward projection, CAS images -> images)."""
+    N = 12
+    p = O.Params(N)
+    rng = np.random.default_rng(21)
+    axes = O.quaternion_axes(5, seed=22)
+    x = rng.standard_normal((N, N, N))
+    y = rng.standard_normal((5, N, N))
+    lhs = np.sum(O.forward_operator(x, axes, p) * y)
+    rhs = np.sum(x * O.forward_adjoint(y, axes, p))
+    assert abs(lhs - rhs) < 1e-10 * abs(lhs)
+
+
 def test_axis_aligned_reference_rule_is_adjoint():
     """For axis-aligned directions the two windows coincide on voxels inside
     the mask sphere (the reference BP writes no voxel outside it, while the
