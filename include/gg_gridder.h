@@ -171,6 +171,26 @@ int gg_back_project_adjoint_kernel(float *d_cas_volume, const float *d_cas_image
                                    const float *d_axes, float ker_hwidth, int n_axes, int cas_vol_size,
                                    int cas_img_size, int mask_radius, int kb_table_size, void *stream);
 
+/* Plane-density-normalised back projection that allocates no memory: writes
+   d_cas_volume_out = BP(d_cas_images) / (BP(all-ones images) + 1e-6), the
+   CAS-volume half of reconstructVol (MultiGPUGridder_Matlab_Class.m:293-308),
+   both back projections under the reference window rule in one fused pass.
+   No counterpart in the reference: its plane density lives in a per-gridder
+   buffer; here it lives in a fixed scratch array in the library's device
+   memory, so the call makes no cudaMalloc, cudaFree or other allocating call.
+   Limit: cas_vol_size^3 <= 4,194,304 (16 MiB of scratch; cas_vol_size <= 161);
+   larger sizes return GG_ERR_INVALID_ARG.  The output is overwritten and need
+   not start at zero; the scratch must be zero when the back projection
+   starts, and the call zeroes it itself on `stream` first.  All calls on one
+   device share the scratch: calls that overlap (different streams or threads
+   with no ordering between them) race on it.  The first call on each device
+   looks up the scratch address (cudaGetSymbolAddress, which may load the
+   library's module onto the device) and should come before any stream
+   capture. */
+int gg_back_project_normalized_noalloc(float *d_cas_volume_out, const float *d_cas_images, const float *d_kb_table,
+                                       const float *d_axes, float ker_hwidth, int n_axes, int cas_vol_size,
+                                       int cas_img_size, int mask_radius, int kb_table_size, void *stream);
+
 /* ---------------------------------------------------------------------------
  * Building blocks: the reference's filters (src/Filters/<name>Filter.cu) on device
  * pointers; `n_slices` = 0 selects the 3-D form where the reference has one.

@@ -71,6 +71,8 @@ SIGNATURES = {
     "gg_forward_project_kernel": (_c_int, [_fp, _fp, _fp, _fp, _c_float, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _vp]),
     "gg_back_project_kernel": (_c_int, [_fp, _fp, _fp, _fp, _c_float, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _vp]),
     "gg_back_project_adjoint_kernel": (_c_int, [_fp, _fp, _fp, _fp, _c_float, _c_int, _c_int, _c_int, _c_int, _c_int, _vp]),
+    "gg_back_project_normalized_noalloc": (_c_int, [_fp, _fp, _fp, _fp, _c_float, _c_int, _c_int, _c_int, _c_int, _c_int,
+                                                    _vp]),
     "gg_filter_complex_to_cas": (_c_int, [_fp, _fp, _c_int, _c_int, _vp]),
     "gg_filter_cas_to_complex": (_c_int, [_fp, _fp, _c_int, _c_int, _vp]),
     "gg_filter_fftshift_2d": (_c_int, [_fp, _c_int, _c_int, _c_int, _vp]),

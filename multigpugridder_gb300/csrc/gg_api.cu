@@ -666,6 +666,8 @@ extern "C" int gg_version(void) { return GG_ABI_VERSION; }
 
 extern "C" const char *gg_global_error(void) { return g_global_err.c_str(); }
 
+void gg::set_global_error(const char *msg) { g_global_err = msg; }
+
 extern "C" const char *gg_last_error(const gg_gridder *h) { return h ? h->err.c_str() : "null gridder handle"; }
 
 extern "C" int gg_create(int volume_size, int num_coord_axes, float interp_factor, int extra_padding, int num_gpus,

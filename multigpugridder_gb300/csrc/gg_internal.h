@@ -107,6 +107,9 @@ cudaError_t launch_storage_scale(const float *d_x, size_t count, float target, u
 // Adds to the process-wide count of kernels launched by this library.
 void count_launches(long long n);
 
+// Sets the calling thread's message returned by gg_global_error().
+void set_global_error(const char *msg);
+
 // ---- host math (gg_kb.cpp) --------------------------------------------------
 void kb_table_f64(int hw, int size, double *out);
 void precomp_f64(int M, int hw, double *out);
