@@ -8,6 +8,7 @@
 // src/Projection/gpuBackProject.cu): x fastest, CAS-volume centre V/2, image
 // centre M/2, nearest-index lookup into the KB table, int mask radius.
 #include <algorithm>
+#include <cmath>
 
 #include "gg_common.cuh"
 #include "gg_internal.h"
@@ -252,8 +253,8 @@ __device__ __forceinline__ float ref_pixel_pos(float pi, float pj, float n_x, fl
 // the reference's roundf(fma(r, kerScale, kerCenter)) for every float r in
 // [-2, 2] (checked exhaustively): both round the same exact value once.
 // INSIDE: the whole window lies in the image, so the reference's
-// linear-index test always passes.
-template <typename TI, bool ONES, bool DENS, bool INSIDE>
+// linear-index test always passes.  Table entry k is read at sker[k * REP].
+template <typename TI, bool ONES, bool DENS, bool INSIDE, int REP = 1>
 __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker, const TI *__restrict__ img_ptr, int M,
                                            int imgi, int imgj, int imgCenter, float &cumSum, float &cumW)
 {
@@ -266,11 +267,11 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
             const int i1 = imgi + io;
             const float pi = (float)(i1 - imgCenter);
             float r = fminf(fmaxf(ref_pixel_pos(pi, pj, q.nx0, q.ny0, q.vc) - q.vi, -2.0f), 2.0f);
-            float w = sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf))];
+            float w = sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf)) * REP];
             r = fminf(fmaxf(ref_pixel_pos(pi, pj, q.nx1, q.ny1, q.vc) - q.vj, -2.0f), 2.0f);
-            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf))]);
+            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf)) * REP]);
             r = fminf(fmaxf(ref_pixel_pos(pi, pj, q.nx2, q.ny2, q.vc) - q.vk, -2.0f), 2.0f);
-            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf))]);
+            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf)) * REP]);
             const int lin = j1 * M + i1;
             if (INSIDE || (lin < M * M && lin >= 0)) {
                 // cumSum += img * w, fused as the reference's build fuses it
@@ -445,52 +446,104 @@ bp_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__re
 }
 
 // ---------------------------------------------------------------------------
-// Back projection, reference window rule, with in-order lane compaction
+// Back projection, reference window rule
 // ---------------------------------------------------------------------------
 // Only the voxels inside a direction's slab (|f_imgk| <= 2, a few percent of
-// the volume) run the 25-pixel window, so a warp that owns one voxel per lane
-// idles about half its lanes.  Here each warp owns 128 voxels (an 8x4x4 block,
-// 4 per lane: slot s = z offset).  Per direction it tests all 128, and the
-// k-th active voxel (slot-major, lane order) is computed by lane k % 32 in
-// round k / 32; each owner lane then takes its voxel's window sum back with a
-// shuffle.  Every voxel still receives its directions one by one in order, so
-// the per-voxel sums are those of the uncompacted kernel, bit for bit.
-constexpr int kCBX = 16, kCBY = 8, kCBZ = 8; // brick: 8 warp blocks of 8x4x4
+// the volume) run the 25-pixel window.  A CTA owns a 16x8x8 brick and each
+// warp an 8x4x4 block of it, 4 voxels per lane: block voxel l = lane + 32 s
+// (x = l & 7, y = (l >> 3) & 3, z = l >> 5).  Per direction a warp tests its
+// 128 voxels against the slab, lists the active ones in shared memory and
+// runs them 32 at a time, one per lane.  Every voxel still receives its
+// directions one by one in order and its window in the reference's order, so
+// the per-voxel sums are those of the reference kernel's loops, bit for bit.
+constexpr int kCBX = 16, kCBY = 8, kCBZ = 8; // brick: 2x2x2 warp blocks of 8x4x4
 constexpr int kCThreads = 256;
+constexpr int kWarpVox = 128;                // voxels per warp block
 
-__device__ __forceinline__ int nth_set_bit(unsigned m, int n)
+// The fast window.  For a voxel coordinate v and a window pixel whose
+// volume-frame position along the same axis is Q, the reference's table
+// index is floor(fma(clamp(fl(Q - v), -2, 2), s, h)), s = kerScale,
+// h = kerCenter + 1/2 (see kb_weight).  For v >= 4 and |Q - v| <= 2,
+// Sterbenz's lemma makes fl(Q - v) = Q - v exact, so that fma and
+// fma(Q, s, h - v*s) round the same real number (h - v*s is exact: s and h
+// are multiples of 1/4); for |Q - v| > 2 both land beyond the same end of the
+// table, where a padded table repeating the edge entries stands in for the
+// clamp.  floor(x) for |x| < 2^22 is the low bits of x + 1.5*2^23 added with
+// round-down.  Checked on the CPU against the reference formula for every
+// float Q within 4.2 of v (v = 4..40; tables of 501 and 1000 entries) and on
+// random samples up to v = 600: identical indices.
+//
+// The pixels come from a per-warp footprint in shared memory: the pixels any
+// window of the warp's block can touch, staged per direction with the
+// reference's linear-index rule (a pixel whose index falls outside the image
+// reads as zero), so the windows read them at constant offsets.
+constexpr int kFootW = 16, kFootH = 16, kFootS = 17; // footprint, row stride
+constexpr int kTabRep = 1;                           // interleaved table copies
+
+__device__ __forceinline__ float lds_f32(unsigned addr)
 {
-    int pos = 0;
-#pragma unroll
-    for (int w = 16; w >= 1; w >>= 1) {
-        const unsigned lo = m & ((1u << w) - 1u);
-        const int c = __popc(lo);
-        if (n >= c) {
-            n -= c;
-            m >>= w;
-            pos += w;
-        } else {
-            m = lo;
-        }
-    }
-    return pos;
+    float v;
+    asm("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
 }
 
+struct FootWin {
+    float nx0, nx1, nx2, ny0, ny1, ny2;
+    float vc;         // volume centre
+    float s;          // kerScale
+    float c0, c1, c2; // h - v*s per axis
+};
+
+// One voxel's 5x5 window from the footprint (fbase = its top-left pixel);
+// table entry floor(x) is read at tab + bits(x + 1.5*2^23) * 4 * kTabRep.
+// Sums in the reference's order.
+template <bool DENS>
+__device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase, unsigned tab, float pi0, float pj0,
+                                            float &cumSum, float &cumW)
+{
+#pragma unroll
+    for (int jo = 0; jo < 5; jo++) {
+        const float pj = pj0 + (float)jo;
+        const float py0 = __fmul_rn(pj, q.ny0), py1 = __fmul_rn(pj, q.ny1), py2 = __fmul_rn(pj, q.ny2);
+#pragma unroll
+        for (int io = 0; io < 5; io++) {
+            const float pi = pi0 + (float)io;
+            const float q0 = __fadd_rn(__fmaf_rn(pi, q.nx0, py0), q.vc);
+            const float q1 = __fadd_rn(__fmaf_rn(pi, q.nx1, py1), q.vc);
+            const float q2 = __fadd_rn(__fmaf_rn(pi, q.nx2, py2), q.vc);
+            const unsigned b0 = __float_as_uint(__fadd_rd(__fmaf_rn(q0, q.s, q.c0), 12582912.0f));
+            const unsigned b1 = __float_as_uint(__fadd_rd(__fmaf_rn(q1, q.s, q.c1), 12582912.0f));
+            const unsigned b2 = __float_as_uint(__fadd_rd(__fmaf_rn(q2, q.s, q.c2), 12582912.0f));
+            float w = lds_f32(tab + b0 * (4u * kTabRep));
+            w = __fmul_rn(w, lds_f32(tab + b1 * (4u * kTabRep)));
+            w = __fmul_rn(w, lds_f32(tab + b2 * (4u * kTabRep)));
+            cumSum = __fmaf_rn(fbase[jo * kFootS + io], w, cumSum);
+            if (DENS) cumW = __fadd_rn(cumW, w);
+        }
+    }
+}
+
+// Table entries below and above the table a window can reach with
+// orthonormal axes: |Q - v| <= sqrt(2.5^2 + 2.5^2 + 2^2) < 4.1 per axis.
+static inline int bp_table_pad(int kerSize) { return (int)ceil(4.25 * (kerSize - 1) / 4.0) + 2; }
+
 template <typename TI, bool ONES, bool DENS>
-__global__ void __launch_bounds__(kCThreads)
+__global__ void __launch_bounds__(kCThreads, 3)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
-                      float kerHW, int bricksX, int bricksY, const float *__restrict__ d_scale)
+                      float kerHW, int bricksX, int bricksY, int tabPad, const float *__restrict__ d_scale)
 {
-    __shared__ float sker[kMaxKerSize];
+    extern __shared__ float stab[]; // (kerSize + 2 tabPad) entries x kTabRep copies
     __shared__ float sax[kBpChunk * 9];
     __shared__ int slist[kBpChunk];
     __shared__ int swarp[kBpChunk / 32];
     __shared__ int scount;
-    // per-voxel sums [warp][slot][lane]; a voxel is updated by at most one lane
-    // per direction, directions in order, so no atomics are needed
-    __shared__ float sacc[kCThreads * 4];
-    __shared__ float saccw[DENS ? kCThreads * 4 : 1];
+    // per-voxel sums [warp][block voxel]; a voxel is updated by at most one
+    // lane per direction, directions in order, so no atomics are needed
+    __shared__ float sacc[kCThreads / 32 * kWarpVox];
+    __shared__ float saccw[DENS ? kCThreads / 32 * kWarpVox : 1];
+    __shared__ float sfoot[kCThreads / 32 * kFootH * kFootS];
+    __shared__ unsigned char svox[kCThreads / 32 * kWarpVox];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int x0 = (blockIdx.x % bricksX) * kCBX;
@@ -506,8 +559,17 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         const float cz = fmaxf(fabsf(z0 + 0.5f * (kCBZ - 1) - volCenter) - 0.5f * (kCBZ - 1), 0.f);
         if (cx * cx + cy * cy + cz * cz > (float)maskR * (float)maskR + 1.0f) return;
     }
-    load_table(sker, ker, kerSize);
+    for (int t = tid; t < (kerSize + 2 * tabPad) * kTabRep; t += kCThreads)
+        stab[t] = __ldg(ker + min(max(t / kTabRep - tabPad, 0), kerSize - 1));
+    const float *sker = stab + tabPad * kTabRep + lane % kTabRep; // entry k at sker[k * kTabRep]
+    const unsigned tab = (unsigned)__cvta_generic_to_shared(stab) + 4u * (unsigned)(lane % kTabRep) +
+                         4u * kTabRep * ((unsigned)tabPad - 0x4B400000u);
+    float *wfoot = sfoot + warp * (kFootH * kFootS);
+    unsigned char *wvox = svox + warp * kWarpVox;
+    float *wacc = sacc + warp * kWarpVox;
+    float *waccw = saccw + (DENS ? warp * kWarpVox : 0);
 
+    // this lane's voxels: x = lx, y = ly, z = bz + s
     const int lx = bx + (lane & 7), ly = by + (lane >> 3);
     const long long R2 = (long long)maskR * maskR;
     unsigned inmask = 0;
@@ -517,21 +579,16 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         const long long d2 = (long long)(lx - volCenter) * (lx - volCenter) + (long long)(ly - volCenter) * (ly - volCenter) +
                              (long long)(lz - volCenter) * (lz - volCenter);
         if (lx < V && ly < V && lz < V && d2 <= R2) inmask |= 1u << s;
+        wacc[lane + 32 * s] = 0.0f;
+        if (DENS) waccw[lane + 32 * s] = 0.0f;
     }
     const float kerCenter = ((float)kerSize - 1) / 2;
     const float kerScale = kerCenter / kerHW;
+    const float kerCenterHalf = kerCenter + 0.5f;
     const float ax0 = (float)lx - volCenter, ay0 = (float)ly - volCenter;
     const float wcx = bx + 3.5f - volCenter, wcy = by + 1.5f - volCenter, wcz = bz + 1.5f - volCenter;
     const float slab = kerHW + kCullEps;
     const int MM = M * M;
-
-#pragma unroll
-    for (int s = 0; s < 4; s++) {
-        sacc[(warp * 4 + s) * 32 + lane] = 0.0f;
-        if (DENS) saccw[(warp * 4 + s) * 32 + lane] = 0.0f;
-    }
-    float *wacc = sacc + warp * 128;
-    float *waccw = saccw + (DENS ? warp * 128 : 0);
     // Directions are staged through shared memory in chunks, culled against
     // the brick (compacted in order), then against each warp's 8x4x4 block.
     const float bcx = x0 + 0.5f * (kCBX - 1) - volCenter, bcy = y0 + 0.5f * (kCBY - 1) - volCenter,
@@ -543,12 +600,23 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         for (int t = tid; t < cn * 9; t += kCThreads) sax[t] = __ldg(axes + (size_t)c0 * 9 + t);
         __syncthreads();
         bool keep = false;
+        int ortho = 0;
         if (tid < cn) {
             const float *ax = sax + tid * 9;
             const float zx = ax[6], zy = ax[7], zz = ax[8];
             const float d = bcx * zx + bcy * zy + bcz * zz;
             const float ext = 0.5f * ((kCBX - 1) * fabsf(zx) + (kCBY - 1) * fabsf(zy) + (kCBZ - 1) * fabsf(zz));
             keep = fabsf(d) <= slab + ext;
+            // the fast window needs orthonormal axes (they bound |Q - v|);
+            // NaN or infinite entries fail these tests
+            const float xx = ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2];
+            const float yy = ax[3] * ax[3] + ax[4] * ax[4] + ax[5] * ax[5];
+            const float zz2 = zx * zx + zy * zy + zz * zz;
+            const float xy = ax[0] * ax[3] + ax[1] * ax[4] + ax[2] * ax[5];
+            const float xz = ax[0] * zx + ax[1] * zy + ax[2] * zz;
+            const float yz = ax[3] * zx + ax[4] * zy + ax[5] * zz;
+            ortho = (fabsf(xx - 1.0f) <= 1e-3f && fabsf(yy - 1.0f) <= 1e-3f && fabsf(zz2 - 1.0f) <= 1e-3f &&
+                     fabsf(xy) <= 1e-3f && fabsf(xz) <= 1e-3f && fabsf(yz) <= 1e-3f) ? kBpChunk : 0;
         }
         const unsigned ballot = __ballot_sync(0xffffffffu, keep);
         if (lane == 0) swarp[warp] = __popc(ballot);
@@ -556,7 +624,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         {
             int off = 0;
             for (int w = 0; w < warp; w++) off += swarp[w];
-            if (keep) slist[off + __popc(ballot & lt_mask)] = tid;
+            if (keep) slist[off + __popc(ballot & lt_mask)] = tid | ortho;
             if (tid == kCThreads - 1) {
                 int tot = 0;
                 for (int w = 0; w < kCThreads / 32; w++) tot += swarp[w];
@@ -567,7 +635,8 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         const int count = scount;
 
         for (int q = 0; q < count; q++) {
-            const int al = slist[q];
+            const int e = slist[q];
+            const int al = e & (kBpChunk - 1);
             const float *ax = sax + al * 9;
             const float nz0 = ax[6], nz1 = ax[7], nz2 = ax[8];
             {   // the warp's 8x4x4 block against the slab (uniform)
@@ -575,48 +644,82 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 const float ext = 0.5f * (7.0f * fabsf(nz0) + 3.0f * fabsf(nz1) + 3.0f * fabsf(nz2));
                 if (fabsf(d) > slab + ext) continue;
             }
-            // the reference's per-voxel slab test (gpuBackProject.cu:64-66) for the 4 slots
-            unsigned b[4];
+            // the reference's per-voxel slab test (gpuBackProject.cu:64-66);
+            // the active voxels are listed slot by slot, in lane order
+            int total = 0;
 #pragma unroll
             for (int s = 0; s < 4; s++) {
-                const float a2 = (float)(bz + s) - volCenter;
-                const float fk = voxel_proj(ax0, ay0, a2, nz0, nz1, nz2);
-                b[s] = __ballot_sync(0xffffffffu, ((inmask >> s) & 1u) && fabsf(fk) <= kerHW);
+                const float az = (float)(bz + s) - volCenter;
+                const float fk = voxel_proj(ax0, ay0, az, nz0, nz1, nz2);
+                const bool act = ((inmask >> s) & 1u) && fabsf(fk) <= kerHW;
+                const unsigned bal = __ballot_sync(0xffffffffu, act);
+                if (act) wvox[total + __popc(bal & lt_mask)] = (unsigned char)(lane + 32 * s);
+                total += __popc(bal);
             }
-            const int p1 = __popc(b[0]), p2 = p1 + __popc(b[1]), p3 = p2 + __popc(b[2]);
-            const int total = p3 + __popc(b[3]);
             if (total == 0) continue;
             const float nx0 = ax[0], nx1 = ax[1], nx2 = ax[2];
             const float ny0 = ax[3], ny1 = ax[4], ny2 = ax[5];
             const TI *img_ptr = img + (size_t)(c0 + al) * MM;
+
+            // this warp's footprint (uniform across the warp)
+            int fi0 = 0, fj0 = 0, fh = 0;
+            bool foot = false;
+            if (e & kBpChunk) {
+                const float ic = wcx * nx0 + wcy * nx1 + wcz * nx2 + (float)imgCenter;
+                const float jc = wcx * ny0 + wcy * ny1 + wcz * ny2 + (float)imgCenter;
+                const float hi = 3.5f * fabsf(nx0) + 1.5f * fabsf(nx1) + 1.5f * fabsf(nx2);
+                const float hj = 3.5f * fabsf(ny0) + 1.5f * fabsf(ny1) + 1.5f * fabsf(ny2);
+                fi0 = (int)floorf(ic - hi - 0.6f) - 2;
+                fj0 = (int)floorf(jc - hj - 0.6f) - 2;
+                const int fw = (int)floorf(ic + hi + 0.6f) + 2 - fi0 + 1;
+                fh = (int)floorf(jc + hj + 0.6f) + 2 - fj0 + 1;
+                foot = fw <= kFootW && fh <= kFootH && fh >= 5;
+                if (foot) {
+                    const int c = lane & (kFootW - 1);
+                    for (int r = lane >> 4; r < fh; r += 2) {
+                        const int lin = (fj0 + r) * M + (fi0 + c);
+                        float v = 0.0f;
+                        if (lin >= 0 && lin < MM) v = ONES ? 1.0f : ld_f32(img_ptr + lin);
+                        wfoot[r * kFootS + c] = v;
+                    }
+                }
+            }
+            __syncwarp();  // the voxel list and the footprint are complete
+
             for (int base = 0; base < total; base += 32) {
                 const int t = base + lane;
                 if (t < total) {
                     float cs = 0.0f, cw = 0.0f;
-                    int s, l;
-                    if (t < p1) { s = 0; l = nth_set_bit(b[0], t); }
-                    else if (t < p2) { s = 1; l = nth_set_bit(b[1], t - p1); }
-                    else if (t < p3) { s = 2; l = nth_set_bit(b[2], t - p2); }
-                    else { s = 3; l = nth_set_bit(b[3], t - p3); }
-                    const int vi = bx + (l & 7), vj = by + (l >> 3), vk = bz + s;
+                    const int l = wvox[t];
+                    const int vi = bx + (l & 7), vj = by + ((l >> 3) & 3), vk = bz + (l >> 5);
                     const float a0 = (float)vi - volCenter, a1 = (float)vj - volCenter, a2 = (float)vk - volCenter;
                     const float f_imgi = __fadd_rn(voxel_proj(a0, a1, a2, nx0, nx1, nx2), (float)imgCenter);
                     const float f_imgj = __fadd_rn(voxel_proj(a0, a1, a2, ny0, ny1, ny2), (float)imgCenter);
                     const int imgi = (int)roundf(f_imgi);
                     const int imgj = (int)roundf(f_imgj);
-                    const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk, (float)volCenter,
-                                       kerScale, kerCenter + 0.5f};
-                    if (imgi >= 2 && imgj >= 2 && imgi + 2 < M && imgj + 2 < M)
-                        ref_window<TI, ONES, DENS, true>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cs, cw);
-                    else
-                        ref_window<TI, ONES, DENS, false>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cs, cw);
+                    const bool inside = imgi >= 2 && imgj >= 2 && imgi + 2 < M && imgj + 2 < M;
+                    const int ri = imgi - 2 - fi0, rj = imgj - 2 - fj0;
+                    if (foot && (unsigned)ri <= (unsigned)(kFootW - 5) && (unsigned)rj <= (unsigned)(fh - 5) &&
+                        vi >= 4 && vj >= 4 && vk >= 4 && (inside || !DENS)) {
+                        const FootWin fwin{nx0, nx1, nx2, ny0, ny1, ny2, (float)volCenter, kerScale,
+                                           kerCenterHalf - (float)vi * kerScale, kerCenterHalf - (float)vj * kerScale,
+                                           kerCenterHalf - (float)vk * kerScale};
+                        foot_window<DENS>(fwin, wfoot + rj * kFootS + ri, tab, (float)(imgi - 2 - imgCenter),
+                                          (float)(imgj - 2 - imgCenter), cs, cw);
+                    } else {
+                        const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk,
+                                           (float)volCenter, kerScale, kerCenterHalf};
+                        if (inside)
+                            ref_window<TI, ONES, DENS, true, kTabRep>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cs, cw);
+                        else
+                            ref_window<TI, ONES, DENS, false, kTabRep>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cs, cw);
+                    }
                     // cumSumAllAxes += cumSum (gpuBackProject.cu:106), in direction order
-                    const int slot = s * 32 + l;
-                    wacc[slot] = __fadd_rn(wacc[slot], cs);
-                    if (DENS) waccw[slot] = __fadd_rn(waccw[slot], cw);
+                    wacc[l] = __fadd_rn(wacc[l], cs);
+                    if (DENS) waccw[l] = __fadd_rn(waccw[l], cw);
                 }
             }
-            __syncwarp();  // the next direction may update these slots from other lanes
+            __syncwarp();  // the next direction rewrites the list, the footprint and these sums
         }
     }
     __syncwarp();
@@ -625,8 +728,8 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     for (int s = 0; s < 4; s++) {
         if (!((inmask >> s) & 1u)) continue;
         const size_t o = (size_t)(bz + s) * V * V + (size_t)ly * V + lx;
-        vol[o] = vol[o] + wacc[s * 32 + lane] * sc;
-        if (DENS) pd[o] = pd[o] + waccw[s * 32 + lane];
+        vol[o] = vol[o] + wacc[lane + 32 * s] * sc;
+        if (DENS) pd[o] = pd[o] + waccw[lane + 32 * s];
     }
 }
 
@@ -637,9 +740,13 @@ static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *k
     if (n <= 0) return cudaSuccess;
     const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
     const long long nb = (long long)bx * by * bz;
-    bp_ref_compact_kernel<TI, ONES, DENS><<<(unsigned)nb, kCThreads, 0, s>>>(vol, pd, g.V, img, g.M, axes, n,
-                                                                             g.mask_radius, ker, g.ker_size, g.ker_hw,
-                                                                             bx, by, scale);
+    const int pad = bp_table_pad(g.ker_size);
+    const size_t dyn = (size_t)(g.ker_size + 2 * pad) * kTabRep * sizeof(float);
+    auto kern = bp_ref_compact_kernel<TI, ONES, DENS>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)nb, kCThreads, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
+                                              g.ker_hw, bx, by, pad, scale);
     count_launches(1);
     return cudaGetLastError();
 }
