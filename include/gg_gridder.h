@@ -42,6 +42,7 @@ extern "C" {
 #define GG_ERR_STATE 4
 #define GG_ERR_NO_DEVICE 5
 #define GG_ERR_CUFFT 6
+#define GG_ERR_TIMEOUT 7 /* gg_server_wait: the request is not done yet */
 
 /* storage precision of the resident CAS volume and of the CAS images the
    projection kernels read (window accumulation is always FP32) */
@@ -233,6 +234,49 @@ int gg_profile_enable(gg_gridder *h, int enable);
 int gg_profile_read(gg_gridder *h, int kernel, double *total_ms, long long *launches);
 
 #ifdef __cplusplus
+/* ---------------------------------------------------------------------------
+ * Serving: a persistent request loop on one GPU.  No counterpart in the
+ * reference, whose calls run one at a time and end with a device sync
+ * (MultiGPUGridder.cpp ForwardProject/BackProject).  A server keeps CAS
+ * volumes resident (each prepared once, as setVolume does) and runs forward and
+ * back projection requests of any volume size and orientation count on
+ * `lanes` CUDA streams: a queued request starts as soon as a lane is free and
+ * its device buffers fit the HBM budget (FIFO admission by footprint), so the
+ * work of requests that arrive while others run overlaps on the device.  A
+ * request's result does not depend on what else runs (same kernels, same
+ * order).  Host buffers should be pinned (cudaHostAlloc) for the copies to
+ * overlap; they must stay valid until gg_server_wait returns.
+ * ------------------------------------------------------------------------- */
+typedef struct gg_server gg_server;
+
+#define GG_OP_FORWARD 0 /* out = forwardProject(volume, axes): n*N*N images */
+#define GG_OP_BACK 1    /* out = backProject(images, axes) into a zeroed CAS volume: V^3 floats */
+
+/* hbm_budget_gb <= 0: 90% of the device memory free at creation. */
+int gg_server_create(int device, double hbm_budget_gb, int lanes, gg_server **out);
+/* Finishes the queued and running requests, then frees everything. */
+void gg_server_destroy(gg_server *s);
+const char *gg_server_last_error(const gg_server *s);
+/* A resident volume (N^3 FP32, host or device pointer), interpolation factor
+   interp_factor, extra padding 3 as the reference's default. */
+int gg_server_add_volume(gg_server *s, const float *volume, int volume_size, float interp_factor, int on_device,
+                         int *volume_id);
+int gg_server_remove_volume(gg_server *s, int volume_id);
+int gg_server_volume_sizes(gg_server *s, int volume_id, int *N, int *M, int *V);
+/* Queues a request; returns at once.  images: n*N*N (GG_OP_BACK only). */
+int gg_server_submit(gg_server *s, int volume_id, int op, const float *axes, int n_axes, const float *images,
+                     float *out, long long *request_id);
+/* Waits for a request (timeout_s < 0: no limit) and returns its status;
+   latency_ms (nullable) = completion - submission.  Each request is waited
+   for once. */
+int gg_server_wait(gg_server *s, long long request_id, double timeout_s, double *latency_ms);
+/* Latency percentiles (submission to completion) of the requests completed
+   since the last reset, the most requests run at once and the most device
+   memory in use (GB, resident volumes included). */
+int gg_server_stats(gg_server *s, long long *completed, double *p50_ms, double *p99_ms, double *mean_ms,
+                    long long *peak_inflight, double *peak_gb);
+int gg_server_reset_stats(gg_server *s);
+
 }
 #endif
 #endif /* GG_GRIDDER_H */

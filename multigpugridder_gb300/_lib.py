@@ -18,6 +18,10 @@ GG_ERR_OUT_OF_MEMORY = 3
 GG_ERR_STATE = 4
 GG_ERR_NO_DEVICE = 5
 GG_ERR_CUFFT = 6
+GG_ERR_TIMEOUT = 7
+
+GG_OP_FORWARD = 0
+GG_OP_BACK = 1
 
 GG_PREC_F32 = 0
 GG_PREC_F16 = 1
@@ -88,6 +92,17 @@ SIGNATURES = {
     "gg_kb_table": (_c_int, [_c_int, _c_int, _dp]),
     "gg_precomp": (_c_int, [_c_int, _c_int, _dp]),
     "gg_kernel_launch_count": (ctypes.c_longlong, []),
+    "gg_server_create": (_c_int, [_c_int, ctypes.c_double, _c_int, ctypes.POINTER(_vp)]),
+    "gg_server_destroy": (None, [_vp]),
+    "gg_server_last_error": (ctypes.c_char_p, [_vp]),
+    "gg_server_add_volume": (_c_int, [_vp, _fp, _c_int, _c_float, _c_int, _ip]),
+    "gg_server_remove_volume": (_c_int, [_vp, _c_int]),
+    "gg_server_volume_sizes": (_c_int, [_vp, _c_int, _ip, _ip, _ip]),
+    "gg_server_submit": (_c_int, [_vp, _c_int, _c_int, _fp, _c_int, _fp, _fp, ctypes.POINTER(ctypes.c_longlong)]),
+    "gg_server_wait": (_c_int, [_vp, ctypes.c_longlong, ctypes.c_double, _dp]),
+    "gg_server_stats": (_c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), _dp, _dp, _dp, ctypes.POINTER(ctypes.c_longlong),
+                                 _dp]),
+    "gg_server_reset_stats": (_c_int, [_vp]),
     "gg_profile_enable": (_c_int, [_vp, _c_int]),
     "gg_profile_read": (_c_int, [_vp, _c_int, _dp, ctypes.POINTER(ctypes.c_longlong)]),
 }

@@ -1206,6 +1206,27 @@ extern "C" int gg_precomp(int M, int ker_hwidth, double *precomp_out)
 
 extern "C" long long gg_kernel_launch_count(void) { return g_launches.load(); }
 
+bool gg::gridder_view(gg_gridder *h, GridderView *out)
+{
+    if (!h || !h->cas.p) return false;
+    std::lock_guard<std::mutex> lock(h->mu);
+    *out = GridderView{h->device, h->N, h->M, h->V, h->geom(), h->cas.p, h->ker.p, h->five_taps};
+    return true;
+}
+
+void gg::gridder_trim(gg_gridder *h)
+{
+    std::lock_guard<std::mutex> lock(h->mu);
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->cs);
+    h->x3.release();
+    h->spec3.release();
+    h->vol_io.release();
+    if (h->have3_r2c) cufftDestroy(h->plan3_r2c);
+    if (h->have3_c2r) cufftDestroy(h->plan3_c2r);
+    h->have3_r2c = h->have3_c2r = false;
+}
+
 extern "C" int gg_profile_enable(gg_gridder *h, int enable)
 {
     return guarded(h, [&] {

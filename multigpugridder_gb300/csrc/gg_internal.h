@@ -110,6 +110,27 @@ void count_launches(long long n);
 // Sets the calling thread's message returned by gg_global_error().
 void set_global_error(const char *msg);
 
+// ---- a gridder's resident state, for the serving loop (gg_api.cu) ---------
+struct GridderView {
+    int device, N, M, V;
+    Geom g;
+    const float *cas; // FP32 CAS volume V^3
+    const float *ker; // KB table
+    bool five_taps;
+};
+
+} // namespace gg
+
+struct gg_gridder;
+
+namespace gg {
+
+// Fills `out` from a gridder whose volume is set; false if it has none.
+bool gridder_view(gg_gridder *h, GridderView *out);
+// Frees the gridder's set-up scratch (the M^3 FFT buffers and plans); the
+// CAS volume stays resident.
+void gridder_trim(gg_gridder *h);
+
 // ---- host math (gg_kb.cpp) --------------------------------------------------
 void kb_table_f64(int hw, int size, double *out);
 void precomp_f64(int M, int hw, double *out);

@@ -1,0 +1,107 @@
+"""The serving loop (gg_server_*): results of a mix of forward and back
+requests on resident volumes of two sizes, submitted all at once so that they
+overlap, equal the same requests run one at a time bit for bit, and equal the
+plain gridder calls (gg_forward_project, gg_back_project + gg_get_cas_volume)
+within relative L2 1e-6 (cuFFT may pick other kernels for other batch
+sizes).  Admission by footprint: a request larger than the HBM budget fails
+with GG_ERR_OUT_OF_MEMORY, and a budget that fits one request at a time runs
+them one at a time."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _requests(vols, seed, count=24):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(count):
+        vid = list(vols)[k % len(vols)]
+        N = vols[vid].shape[0]
+        n = int(np.exp(rng.uniform(np.log(1), np.log(300))))
+        op = "back" if rng.random() < 0.5 else "forward"
+        axes = O.quaternion_axes(n, seed * 1000 + k).astype(np.float32)
+        imgs = rng.standard_normal((n, N, N)).astype(np.float32) if op == "back" else None
+        reqs.append((vid, op, axes, imgs))
+    return reqs
+
+
+def _plain(L, vol, op, axes, imgs):
+    N = vol.shape[0]
+    h = ctypes.c_void_p()
+    dev = (ctypes.c_int * 1)(0)
+    assert L.gg_create(N, 0, ctypes.c_float(2.0), 3, 1, dev, 1, 0, ctypes.byref(h)) == 0
+    dims = (ctypes.c_int * 3)(N, N, N)
+    n = len(axes)
+    try:
+        if op == "forward":
+            assert L.gg_set_volume(h, vol.ctypes.data, dims) == 0
+            out = np.empty((n, N, N), np.float32)
+            assert L.gg_forward_project(h, axes.ctypes.data, n, out.ctypes.data, None) == 0
+        else:
+            Nn, M, V, R = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            L.gg_get_sizes(h, ctypes.byref(Nn), ctypes.byref(M), ctypes.byref(V), ctypes.byref(R))
+            assert L.gg_back_project(h, axes.ctypes.data, n, imgs.ctypes.data, None, 0) == 0
+            out = np.empty((V.value,) * 3, np.float32)
+            assert L.gg_get_cas_volume(h, out.ctypes.data) == 0
+    finally:
+        L.gg_destroy(h)
+    return out
+
+
+def test_mix_equals_alone_and_plain_path(cuda, gglib):
+    from multigpugridder_gb300.serve import Server
+
+    vols = {}
+    with Server(lanes=4) as srv:
+        for N, seed in ((16, 61), (24, 62)):
+            v = O.blob_volume(N, 6, seed=seed).astype(np.float32)
+            vols[srv.add_volume(v)] = v
+        reqs = _requests(vols, seed=63)
+        # all at once: they overlap on the lanes
+        handles = [srv.submit(vid, op, axes, imgs) for vid, op, axes, imgs in reqs]
+        mixed = [srv.wait(h)[0].copy() for h in handles]
+        st = srv.stats()
+        assert st["completed"] == len(reqs)
+        assert st["peak_inflight"] > 1
+        # one at a time
+        alone = []
+        for vid, op, axes, imgs in reqs:
+            alone.append(srv.wait(srv.submit(vid, op, axes, imgs))[0].copy())
+    for (vid, op, axes, imgs), a, b in zip(reqs, mixed, alone):
+        assert np.array_equal(a, b), (op, len(axes))
+        assert np.all(np.isfinite(a))
+    for k in (0, 1, 2, 3, 5, 8):
+        vid, op, axes, imgs = reqs[k]
+        ref = _plain(gglib, vols[vid], op, axes, imgs)
+        assert O.rel_l2(mixed[k], ref) < 1e-6, (op, len(axes))
+
+
+def test_admission_by_footprint(cuda):
+    from multigpugridder_gb300 import _lib
+    from multigpugridder_gb300._lib import GridderError
+    from multigpugridder_gb300.serve import Server
+
+    v = O.blob_volume(24, 6, seed=64).astype(np.float32)
+    axes = O.quaternion_axes(64, 65).astype(np.float32)
+    imgs = np.random.default_rng(66).standard_normal((64, 24, 24)).astype(np.float32)
+    # a budget that holds the volume and one back request (~3.5 MB), not two
+    with Server(hbm_budget_gb=0.0045, lanes=4) as srv:
+        vid = srv.add_volume(v)
+        hs = [srv.submit(vid, "back", axes, imgs) for _ in range(4)]
+        outs = [srv.wait(h)[0].copy() for h in hs]
+        assert srv.stats()["peak_inflight"] == 1
+        for o in outs[1:]:
+            assert np.array_equal(o, outs[0])
+        big = srv.submit(vid, "back", O.quaternion_axes(4096, 67).astype(np.float32),
+                         np.zeros((4096, 24, 24), np.float32))
+        with pytest.raises(GridderError) as e:
+            srv.wait(big)
+        assert e.value.code == _lib.GG_ERR_OUT_OF_MEMORY
+        # the server keeps serving
+        out, _ = srv.wait(srv.submit(vid, "forward", axes[:5]))
+        assert out.shape == (5, 24, 24) and np.all(np.isfinite(out))
