@@ -49,20 +49,26 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=64)
+    ap.add_argument("--serve-seconds", type=float, default=2.0,
+                    help="arrival window of the serving workload (0: skip it)")
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (Poisson)")
+    ap.add_argument("--serve-lanes", type=int, default=8)
+    ap.add_argument("--serve-closed", type=int, default=200,
+                    help="requests in the closed-loop served vs sequential plain-path comparison")
     return ap.parse_args()
 
 
 def workload(args):
-    from oracle import oracle as O  # seeded synthetic inputs only (no checking here)
+    from multigpugridder_gb300 import synthetic
 
     N = args.size
     n_blobs = 100 if N == 128 else max(10, N // 2)
-    vol = O.blob_volume(N, n_blobs, seed=2)
+    vol = synthetic.blob_volume(N, n_blobs, seed=2)
     side = int(round(args.directions ** 0.5))
     if side * side == args.directions:
-        axes = O.grid_axes(side, side).astype(np.float32)
+        axes = synthetic.grid_axes(side, side).astype(np.float32)
     else:
-        axes = O.quaternion_axes(args.directions, seed=2).astype(np.float32)
+        axes = synthetic.quaternion_axes(args.directions, seed=2).astype(np.float32)
     return vol, axes
 
 
@@ -283,6 +289,9 @@ def run_gb300(args):
                 "sample": "%d of %d directions timed, step extrapolated (t_fixed + D/S * t_sample)" % (S, n)}
 
     g.close()
+    serve = None
+    if rank == 0 and world == 1 and args.serve_seconds > 0:
+        serve = run_serve(args)
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -295,10 +304,146 @@ def run_gb300(args):
                           "l2": "inputs larger than L2 (10,000 images = %d MB per step) and an untimed %d MB "
                                 "write between steps" % (n * N * N * 4 >> 20, flush.numel() * 4 >> 20)},
                "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
-               "clocks": clk, "step_ms": ms_steps}
+               "clocks": clk, "step_ms": ms_steps, "serve": serve}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+# ---- serving workload ---------------------------------------------------------
+SERVE_SIZES = (64, 128, 192, 256)
+SERVE_WEIGHTS = (0.4, 0.3, 0.2, 0.1)
+SERVE_BLOBS = (20, 100, 200, 400)
+
+
+def serve_schedule(seconds, rate, seed=5, count=None):
+    """(arrival s, size index, op, directions, request seed): Poisson arrivals,
+    sizes 64/128/192/256 with weights .4/.3/.2/.1, forward/back 50/50,
+    directions log-uniform in 16..4096."""
+    rng = np.random.default_rng(seed)
+    out, t, k = [], 0.0, 0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if (count is None and t >= seconds) or (count is not None and k >= count):
+            break
+        si = int(rng.choice(4, p=SERVE_WEIGHTS))
+        op = "forward" if rng.random() < 0.5 else "back"
+        n = int(np.exp(rng.uniform(np.log(16), np.log(4096))))
+        out.append((t, si, op, n, 1000 + k))
+        k += 1
+    return out
+
+
+def run_serve(args):
+    """Open-loop Poisson serving at the offered rate and at 70% of the
+    measured capacity, and a closed-loop comparison with sequential
+    plain-path calls (gg_forward_project / gg_back_project + gg_get_cas_volume)."""
+    from multigpugridder_gb300 import synthetic
+    from multigpugridder_gb300._lib import check, lib
+    from multigpugridder_gb300.serve import Server, pinned_empty
+
+    L = lib()
+    offered = serve_schedule(args.serve_seconds, args.serve_rate)
+    closed = offered[:args.serve_closed]
+    axes = {}
+    for sched in (offered,):
+        for _, _, _, n, seed in sched:
+            if seed not in axes:
+                axes[seed] = synthetic.quaternion_axes(n, seed).astype(np.float32)
+    vols = [synthetic.blob_volume(N, b, seed=50 + i) for i, (N, b) in enumerate(zip(SERVE_SIZES, SERVE_BLOBS))]
+    srv = Server(lanes=args.serve_lanes)
+    vids = [srv.add_volume(v) for v in vols]
+    sizes = [srv.sizes(v) for v in vids]
+    rng = np.random.default_rng(7)
+    img_in, fp_out, bp_out = [], [], []
+    for (N, M, V) in sizes:
+        block = rng.standard_normal((64, N, N)).astype(np.float32)
+        buf = pinned_empty((4096, N, N))
+        buf[:] = np.resize(block, buf.shape)
+        img_in.append(buf.reshape(-1))
+        fp_out.append(pinned_empty((4096 * N * N,)))
+        bp_out.append(pinned_empty((V * V * V,)))
+
+    def submit(si, op, n, seed):
+        N, M, V = sizes[si]
+        ax = axes[seed][:n]
+        if op == "forward":
+            return srv.submit(vids[si], op, ax, out=fp_out[si][:n * N * N])
+        return srv.submit(vids[si], op, ax, images=img_in[si][:n * N * N], out=bp_out[si])
+
+    def open_loop(sched, scale=1.0):
+        srv.reset_stats()
+        t0 = time.perf_counter()
+        hs = []
+        for t, si, op, n, seed in sched:
+            t = t * scale
+            while True:
+                dt = t - (time.perf_counter() - t0)
+                if dt <= 0:
+                    break
+                if dt > 2e-3:
+                    time.sleep(dt - 1e-3)
+            hs.append(submit(si, op, n, seed))
+        for h in hs:
+            srv.wait(h)
+        el = time.perf_counter() - t0
+        st = srv.stats()
+        dirs = sum(x[3] for x in sched)
+        return {"offered_rps": len(sched) / (sched[-1][0] * scale) if sched else 0.0, "requests": len(sched),
+                "seconds": el, "throughput_rps": len(sched) / el, "directions_per_s": dirs / el,
+                "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+                "peak_inflight": st["peak_inflight"], "peak_gb": st["peak_gb"]}
+
+    # warm the lanes, then the closed loop: all requests queued at once
+    for h in [submit(si, op, min(n, 64), seed) for _, si, op, n, seed in closed[:16]]:
+        srv.wait(h)
+    t0 = time.perf_counter()
+    hs = [submit(si, op, n, seed) for _, si, op, n, seed in closed]
+    for h in hs:
+        srv.wait(h)
+    served_closed = len(closed) / (time.perf_counter() - t0)
+    # the same requests one at a time through the plain gridder calls
+    grids = []
+    for v, (N, M, V) in zip(vols, sizes):
+        h = ctypes.c_void_p()
+        dev = (ctypes.c_int * 1)(0)
+        check(L.gg_create(N, 0, ctypes.c_float(2.0), 3, 1, dev, 1, 0, ctypes.byref(h)))
+        check(L.gg_set_max_axes_to_allocate(h, 4096), h)
+        dims = (ctypes.c_int * 3)(N, N, N)
+        check(L.gg_set_volume(h, v.ctypes.data, dims), h)
+        grids.append(h)
+
+    def plain(si, op, n, seed):
+        h = grids[si]
+        N, M, V = sizes[si]
+        ax = axes[seed]
+        if op == "forward":
+            check(L.gg_forward_project(h, ax.ctypes.data, n, fp_out[si].ctypes.data, None), h)
+        else:
+            check(L.gg_back_project(h, ax.ctypes.data, n, img_in[si].ctypes.data, None, 0), h)
+            check(L.gg_get_cas_volume(h, bp_out[si].ctypes.data), h)
+
+    for _, si, op, n, seed in closed[:16]:
+        plain(si, op, min(n, 64), seed)
+    t0 = time.perf_counter()
+    for _, si, op, n, seed in closed:
+        plain(si, op, n, seed)
+    seq_closed = len(closed) / (time.perf_counter() - t0)
+    for h in grids:
+        L.gg_destroy(h)
+
+    res_offered = open_loop(offered)
+    cap = res_offered["throughput_rps"]
+    rate70 = 0.7 * min(cap, args.serve_rate)
+    res_70 = open_loop(offered[:max(1, int(rate70 * args.serve_seconds))], scale=args.serve_rate / rate70)
+    srv.close()
+    return {"workload": "Poisson arrivals at %g req/s for %g s: forwardProject/backProject 50/50 on resident FP32 "
+                        "volumes 64^3/128^3/192^3/256^3 (weights .4/.3/.2/.1, interpFactor 2), directions "
+                        "log-uniform 16-4096 (random quaternions); back requests return the CAS volume"
+                        % (args.serve_rate, args.serve_seconds),
+            "lanes": args.serve_lanes, "offered": res_offered, "at_70pct_capacity": res_70,
+            "closed_loop": {"requests": len(closed), "served_rps": served_closed, "sequential_plain_rps": seq_closed,
+                            "speedup": served_closed / seq_closed}}
 
 
 def run_e2e(args, g, vol, axes, world):

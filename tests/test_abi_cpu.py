@@ -93,3 +93,16 @@ def test_interp_factor_adjustment():
     assert adjust_interp_factor(128, 2) == 2.0
     assert adjust_interp_factor(208, 2) == pytest.approx(512 / 208)
     assert adjust_interp_factor(256, 2) == 2.0
+
+
+def test_synthetic_inputs_match_the_oracle_generators():
+    """The package's seeded generators (used by the benchmark) give the
+    oracle's volumes and directions."""
+    import numpy as np
+
+    from multigpugridder_gb300 import synthetic
+    from oracle import oracle as O
+
+    assert np.array_equal(synthetic.blob_volume(24, 10, seed=5), O.blob_volume(24, 10, seed=5))
+    assert np.array_equal(synthetic.quaternion_axes(64, 6).astype(np.float32), O.quaternion_axes(64, 6).astype(np.float32))
+    assert np.array_equal(synthetic.grid_axes(12, 10).astype(np.float32), O.grid_axes(12, 10).astype(np.float32))
