@@ -1,8 +1,8 @@
 // Host engine and C ABI of the GB300 gridder (include/gg_gridder.h).
 //
-// One handle owns one GPU's state: the resident FP32 CAS volume (plus an
-// FP16/BF16 copy for the forward projection when reduced-precision storage is
-// selected), the KB table and pre-compensation vector, batch buffers and
+// One handle owns one GPU's state: the resident FP32 CAS volume (plus the
+// copy the forward projection reads: rows padded for aligned vector loads, in
+// the selected storage precision), the KB table and pre-compensation vector, batch buffers and
 // cached cuFFT plans.  It replaces the reference's MultiGPUGridder /
 // gpuGridder / AbstractGridder trio (src/Gridders/) for one device:
 //   * the volume is prepared on the device once per setVolume instead of on
@@ -148,8 +148,9 @@ struct gg_gridder {
     DevBuf<float> ker;
     DevBuf<double> precomp;
     DevBuf<float> cas;       // FP32 CAS volume V^3 (resident)
-    DevBuf<uint16_t> cas_lp; // FP16/BF16 copy read by the forward projection
-    bool cas_lp_valid = false;
+    DevBuf<float> cas_fp;    // the CAS volume as the forward projection reads it: row pitch
+                             // fp_pitch(V), storage `prec` (FP16 scaled by scales[0])
+    bool cas_fp_valid = false;
     DevBuf<float> pd;        // plane density V^3
     DevBuf<float> adj;       // CAS-volume gradient V^3 (forward-operator adjoint)
     DevBuf<float> axes;
@@ -296,15 +297,17 @@ void check_axes_count(int n)
     if (n < 0) fail(GG_ERR_INVALID_ARG, "n_axes must be >= 0 (got %d)", n);
 }
 
-// Refresh the reduced-precision copy of the CAS volume read by the forward projection.
-void update_lp(gg_gridder *h, cudaStream_t s)
+// Refresh the copy of the CAS volume read by the forward projection (pitched
+// rows, storage precision).
+void update_fp(gg_gridder *h, cudaStream_t s)
 {
-    if (h->prec == kF32 || h->cas_lp_valid) return;
+    if (h->cas_fp_valid) return;
     const size_t V3 = (size_t)h->V * h->V * h->V;
-    h->cas_lp.ensure(V3);
+    const int P = fp_pitch(h->V);
+    h->cas_fp.ensure(((size_t)P * h->V * h->V * prec_bytes(h->prec) + 3) / 4);
     if (h->prec == kF16) GG_CK(launch_storage_scale(h->cas.p, V3, 8192.0f, h->work.p, h->scales.p, s));
-    GG_CK(launch_convert(h->cas.p, h->cas_lp.p, h->prec, V3, h->vol_scale(), s));
-    h->cas_lp_valid = true;
+    GG_CK(launch_pitch_volume(h->cas.p, h->V, P, h->cas_fp.p, h->prec, h->vol_scale(), s));
+    h->cas_fp_valid = true;
 }
 
 // ---- device-side pipelines (all on stream s) --------------------------------
@@ -321,7 +324,7 @@ void do_set_volume(gg_gridder *h, const float *d_vol, cudaStream_t s)
     GG_CKF(cufftSetStream(p, s));
     GG_CKF(cufftExecR2C(p, h->x3.p, h->spec3.p));
     GG_CK(launch_spectrum_to_cas_volume(h->spec3.p, h->M, h->V, h->cas.p, kF32, nullptr, s));
-    h->cas_lp_valid = false;
+    h->cas_fp_valid = false;
 }
 
 void do_get_volume(gg_gridder *h, const float *d_cas, float *d_vol, cudaStream_t s)
@@ -341,9 +344,9 @@ void do_get_volume(gg_gridder *h, const float *d_cas, float *d_vol, cudaStream_t
 void fp_batch(gg_gridder *h, const float *d_axes, int b, float *cas_out, float *img_out, int sl, cudaStream_t s)
 {
     auto &S = h->slot[sl];
-    const void *vol = h->prec == kF32 ? (const void *)h->cas.p : (const void *)h->cas_lp.p;
     ProfScope ps(h, s, GG_KERNEL_FORWARD);
-    GG_CK(launch_forward_project(vol, h->prec, cas_out, h->ker.p, d_axes, b, h->geom(), h->five_taps, h->vol_scale(), s));
+    GG_CK(launch_forward_project(h->cas_fp.p, h->prec, fp_pitch(h->V), cas_out, h->ker.p, d_axes, b, h->geom(),
+                                 h->five_taps, h->vol_scale(), s));
     ps.done();
     if (img_out) {
         GG_CK(launch_cas_images_to_spectrum(cas_out, h->M, b, S.spec.p, s));
@@ -458,7 +461,7 @@ void fp_host(gg_gridder *h, const float *axes, int n, float *images_out, float *
 {
     cudaStream_t cs = h->cs, cp = h->cp;
     upload_axes(h, axes, n, cs);
-    update_lp(h, cs);
+    update_fp(h, cs);
     const int B = h->max_batch;
     const size_t MM = (size_t)h->M * h->M, NN = (size_t)h->N * h->N;
     const bool pin_img = images_out && host_is_pinned(images_out);
@@ -597,7 +600,7 @@ void destroy_handle(gg_gridder *h)
     h->ker.release();
     h->precomp.release();
     h->cas.release();
-    h->cas_lp.release();
+    h->cas_fp.release();
     h->pd.release();
     h->adj.release();
     h->axes.release();
@@ -799,7 +802,7 @@ extern "C" int gg_set_precision(gg_gridder *h, int precision)
         if (precision != h->prec) {
             GG_CK(cudaStreamSynchronize(h->cs));
             h->prec = precision;
-            h->cas_lp_valid = false;
+            h->cas_fp_valid = false;
             for (auto &S : h->slot) S.casimg_lp.release();
         }
     });
@@ -837,7 +840,7 @@ extern "C" int gg_set_cas_volume(gg_gridder *h, const float *cas_volume, const i
         h->cas.ensure(V3);
         GG_CK(cudaMemcpyAsync(h->cas.p, cas_volume, V3 * sizeof(float), cudaMemcpyHostToDevice, h->cs));
         GG_CK(cudaStreamSynchronize(h->cs));
-        h->cas_lp_valid = false;
+        h->cas_fp_valid = false;
     });
 }
 
@@ -859,7 +862,7 @@ extern "C" int gg_reset_volume(gg_gridder *h)
         h->cas.ensure(V3);
         GG_CK(cudaMemsetAsync(h->cas.p, 0, V3 * sizeof(float), h->cs));
         GG_CK(cudaStreamSynchronize(h->cs));
-        h->cas_lp_valid = false;
+        h->cas_fp_valid = false;
     });
 }
 
@@ -887,7 +890,7 @@ extern "C" int gg_back_project(gg_gridder *h, const float *axes, int n_axes, con
         if (!accumulate) GG_CK(cudaMemsetAsync(h->cas.p, 0, V3 * sizeof(float), h->cs));
         if (n_axes > 0) bp_host(h, axes, n_axes, images, cas_images, h->cas.p, false);
         GG_CK(cudaStreamSynchronize(h->cs));
-        h->cas_lp_valid = false;
+        h->cas_fp_valid = false;
     });
 }
 
@@ -923,7 +926,7 @@ extern "C" int gg_reconstruct_volume(gg_gridder *h, const float *axes, int n_axe
         do_get_volume(h, h->cas.p, h->vol_io.p, h->cs);
         GG_CK(cudaMemcpyAsync(volume_out, h->vol_io.p, N3 * sizeof(float), cudaMemcpyDeviceToHost, h->cs));
         GG_CK(cudaStreamSynchronize(h->cs));
-        h->cas_lp_valid = false;
+        h->cas_fp_valid = false;
     });
 }
 
@@ -949,7 +952,7 @@ extern "C" int gg_set_cas_volume_dev(gg_gridder *h, const float *d_cas_volume, v
         const size_t V3 = (size_t)h->V * h->V * h->V;
         h->cas.ensure(V3);
         GG_CK(cudaMemcpyAsync(h->cas.p, d_cas_volume, V3 * sizeof(float), cudaMemcpyDeviceToDevice, s));
-        h->cas_lp_valid = false;
+        h->cas_fp_valid = false;
         end_dev(h, s);
     });
 }
@@ -978,7 +981,7 @@ extern "C" int gg_forward_project_dev(gg_gridder *h, const float *d_axes, int n_
         if (n_axes == 0) return;
         cudaStream_t s = (cudaStream_t)stream;
         begin_dev(h, s);
-        update_lp(h, s);
+        update_fp(h, s);
         const int B = h->max_batch;
         const size_t MM = (size_t)h->M * h->M, NN = (size_t)h->N * h->N;
         for (int a0 = 0; a0 < n_axes; a0 += B) {
@@ -1011,7 +1014,7 @@ extern "C" int gg_back_project_dev(gg_gridder *h, const float *d_axes, int n_axe
             bp_batch(h, d_axes + (size_t)a0 * 9, b, d_images ? d_images + (size_t)a0 * NN : nullptr,
                      d_cas_images ? d_cas_images + (size_t)a0 * MM : nullptr, h->cas.p, false, 0, s);
         }
-        h->cas_lp_valid = false;
+        h->cas_fp_valid = false;
         end_dev(h, s);
     });
 }
@@ -1050,7 +1053,7 @@ extern "C" int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int
         }
         GG_CK(launch_divide_plane_density(h->cas.p, h->pd.p, V3, 1e-6f, s));
         do_get_volume(h, h->cas.p, d_volume_out, s);
-        h->cas_lp_valid = false;
+        h->cas_fp_valid = false;
         end_dev(h, s);
     });
 }
@@ -1132,7 +1135,7 @@ extern "C" int gg_forward_project_kernel(const float *d_cas_volume, float *d_cas
     }
     const bool five = !table_has_zero_edges(d_kb_table, kb_table_size);
     Geom g{cas_vol_size, cas_img_size, mask_radius, kb_table_size, ker_hwidth};
-    cudaError_t e = launch_forward_project(d_cas_volume, kF32, d_cas_images, d_kb_table, d_axes, n_axes, g, five, nullptr,
+    cudaError_t e = launch_forward_project(d_cas_volume, kF32, cas_vol_size, d_cas_images, d_kb_table, d_axes, n_axes, g, five, nullptr,
                                            (cudaStream_t)stream);
     if (e != cudaSuccess) {
         g_global_err = cudaGetErrorString(e);

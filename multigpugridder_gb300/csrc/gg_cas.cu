@@ -289,6 +289,19 @@ __global__ void convert_kernel(const float *__restrict__ in, T *__restrict__ out
         out[e] = from_f32<T>(in[e] * inv_scale);
 }
 
+template <typename T>
+__global__ void pitch_volume_kernel(const float *__restrict__ cas, int V, int P, T *__restrict__ out,
+                                    const float *__restrict__ d_scale)
+{
+    const float inv_scale = d_scale ? 1.0f / *d_scale : 1.0f;
+    const size_t total = (size_t)V * V * P;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = e / P;
+        const int i = (int)(e - row * P);
+        out[e] = from_f32<T>(i < V ? cas[row * V + i] * inv_scale : 0.0f);
+    }
+}
+
 // Non-negative floats order like their bit patterns, so an unsigned atomicMax
 // on the bits of |x| finds the largest magnitude.
 __global__ void max_abs_kernel(const float *__restrict__ x, size_t count, unsigned int *out)
@@ -430,6 +443,17 @@ cudaError_t launch_convert(const float *d_in, void *d_out, int prec, size_t coun
     if (prec == kF32) convert_kernel<float><<<g, kT, 0, s>>>(d_in, (float *)d_out, count, d_scale);
     else if (prec == kF16) convert_kernel<__half><<<g, kT, 0, s>>>(d_in, (__half *)d_out, count, d_scale);
     else convert_kernel<__nv_bfloat16><<<g, kT, 0, s>>>(d_in, (__nv_bfloat16 *)d_out, count, d_scale);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pitch_volume(const float *d_cas, int V, int P, void *d_out, int prec, const float *d_scale,
+                                cudaStream_t s)
+{
+    const unsigned g = grid_for((size_t)V * V * P, kT);
+    if (prec == kF32) pitch_volume_kernel<float><<<g, kT, 0, s>>>(d_cas, V, P, (float *)d_out, d_scale);
+    else if (prec == kF16) pitch_volume_kernel<__half><<<g, kT, 0, s>>>(d_cas, V, P, (__half *)d_out, d_scale);
+    else pitch_volume_kernel<__nv_bfloat16><<<g, kT, 0, s>>>(d_cas, V, P, (__nv_bfloat16 *)d_out, d_scale);
     count_launches(1);
     return cudaGetLastError();
 }

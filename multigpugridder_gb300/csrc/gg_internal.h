@@ -30,9 +30,17 @@ struct Geom {
 // Storage scaling: FP16 storage holds x / scale, with scale a power of two
 // kept in device memory (d_scale; NULL means 1) so no host sync is needed.
 // The forward projection multiplies every output pixel by *d_scale.
-cudaError_t launch_forward_project(const void *d_vol, int vprec, float *d_img, const float *d_ker,
+// The volume's rows are `pitch` elements apart (planes pitch*V); the
+// reference's dense layout is pitch = V.  fp_pitch(V) rows let the 4-tap
+// kernel read each row of taps with aligned vector loads.
+cudaError_t launch_forward_project(const void *d_vol, int vprec, int pitch, float *d_img, const float *d_ker,
                                    const float *d_axes, int n, const Geom &g, bool five_taps,
                                    const float *d_scale, cudaStream_t s);
+inline int fp_pitch(int V) { return (V + 4 + 7) / 8 * 8; }
+// FP32 CAS volume V^3 -> the same volume with row pitch P (zero-filled past
+// V) in storage `prec` (x / *d_scale for FP16).
+cudaError_t launch_pitch_volume(const float *d_cas, int V, int P, void *d_out, int prec, const float *d_scale,
+                                cudaStream_t s);
 
 // Back projection with the reference window rule, accumulated (+=) into the
 // FP32 CAS volume.  d_img holds n*M*M CAS images in storage `iprec`; when

@@ -79,12 +79,53 @@ static int num_sms()
 // round(f) (gpuForwardProject.cu:63-98) the fifth always has |r| >= 2, is
 // clamped to the table edge and weighs exactly zero.  TAPS = 5 keeps the
 // reference's full window for tables without zero edges.
+//
+// The volume may be stored with a row pitch P >= V (plane pitch P*V; the
+// reference's dense layout is P = V).  VEC (2-byte storage, 4 taps, P a
+// multiple of 8, P >= V + 4): each row of 4 taps is read as the 8 elements from the 4-aligned
+// x at or below floor(f) - 1 in two aligned vector loads, and the 4 x weights
+// are placed at their offsets in an 8-wide weight vector (zeros elsewhere) once
+// per pixel.  The extra terms are exact zeros, so the sums are those of the
+// 4 scalar taps, bit for bit, for a finite volume.
 constexpr int kFpTile = 16;
 constexpr int kFpThreads = 256;
 
-template <typename TV, int TAPS>
+__device__ __forceinline__ void ld8(const float *p, float v[8])
+{
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(p));
+    const float4 b = __ldg(reinterpret_cast<const float4 *>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+__device__ __forceinline__ void ld8(const __half *p, float v[8])
+{
+    const uint2 a = __ldg(reinterpret_cast<const uint2 *>(p));
+    const uint2 b = __ldg(reinterpret_cast<const uint2 *>(p) + 1);
+    const unsigned w[4] = {a.x, a.y, b.x, b.y};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const float2 f = __half22float2(*reinterpret_cast<const __half2 *>(&w[q]));
+        v[2 * q] = f.x;
+        v[2 * q + 1] = f.y;
+    }
+}
+
+__device__ __forceinline__ void ld8(const __nv_bfloat16 *p, float v[8])
+{
+    const uint2 a = __ldg(reinterpret_cast<const uint2 *>(p));
+    const uint2 b = __ldg(reinterpret_cast<const uint2 *>(p) + 1);
+    const unsigned w[4] = {a.x, a.y, b.x, b.y};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        v[2 * q] = __uint_as_float(w[q] << 16);
+        v[2 * q + 1] = __uint_as_float(w[q] & 0xFFFF0000u);
+    }
+}
+
+template <typename TV, int TAPS, bool VEC>
 __global__ void __launch_bounds__(kFpThreads)
-fp_kernel(const TV *__restrict__ vol, int V, float *__restrict__ img, int M,
+fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int M,
           const float *__restrict__ axes, int maskR, const float *__restrict__ ker, int kerSize,
           float kerHW, int tilesX, long long nItems, const float *__restrict__ d_scale)
 {
@@ -103,7 +144,7 @@ fp_kernel(const TV *__restrict__ vol, int V, float *__restrict__ img, int M,
     const float convW = (float)(int)roundf(kerHW);
     const long long R2 = (long long)maskR * maskR;
     const int tilesPerImg = tilesX * tilesX;
-    const size_t VV = (size_t)V * V;
+    const size_t VV = (size_t)V * V, PV = (size_t)P * V;
     const long long V3 = (long long)VV * V;
 
     for (long long item = blockIdx.x; item < nItems; item += gridDim.x) {
@@ -152,13 +193,32 @@ fp_kernel(const TV *__restrict__ vol, int V, float *__restrict__ img, int M,
 
         float acc = 0.0f;
         const bool inside = b0 >= 0 && b1 >= 0 && b2 >= 0 && b0 + TAPS <= V && b1 + TAPS <= V && b2 + TAPS <= V;
-        if (inside) {
-            const TV *base = vol + (size_t)b2 * VV + (size_t)b1 * V + b0;
+        if (VEC && inside) {
+            const int sft = b0 & 3;
+            float w8[8];
+#pragma unroll
+            for (int t = 0; t < 8; t++)
+                w8[t] = t == sft ? wi[0] : t == sft + 1 ? wi[1] : t == sft + 2 ? wi[2] : t == sft + 3 ? wi[3] : 0.0f;
+            const TV *base = vol + (size_t)b2 * PV + (size_t)b1 * P + (b0 - sft);
 #pragma unroll
             for (int dk = 0; dk < TAPS; dk++) {
 #pragma unroll
                 for (int dj2 = 0; dj2 < TAPS; dj2++) {
-                    const TV *p = base + (size_t)dk * VV + (size_t)dj2 * V;
+                    float v[8];
+                    ld8(base + (size_t)dk * PV + (size_t)dj2 * P, v);
+                    float s = 0.0f;
+#pragma unroll
+                    for (int t = 0; t < 8; t++) s = fmaf(w8[t], v[t], s);
+                    acc = fmaf(wj[dj2] * wk[dk], s, acc);
+                }
+            }
+        } else if (inside) {
+            const TV *base = vol + (size_t)b2 * PV + (size_t)b1 * P + b0;
+#pragma unroll
+            for (int dk = 0; dk < TAPS; dk++) {
+#pragma unroll
+                for (int dj2 = 0; dj2 < TAPS; dj2++) {
+                    const TV *p = base + (size_t)dk * PV + (size_t)dj2 * P;
                     float s = 0.0f;
 #pragma unroll
                     for (int d = 0; d < TAPS; d++) s = fmaf(wi[d], ld_f32(p + d), s);
@@ -166,49 +226,60 @@ fp_kernel(const TV *__restrict__ vol, int V, float *__restrict__ img, int M,
                 }
             }
         } else {
-            // Near the volume edge: the reference's linear-index test
-            // (gpuForwardProject.cu:90), plus a lower bound.
+            // Near the volume edge: the reference's linear-index test on the
+            // dense layout (gpuForwardProject.cu:90), plus a lower bound.
             for (int dk = 0; dk < TAPS; dk++)
                 for (int dj2 = 0; dj2 < TAPS; dj2++)
                     for (int d = 0; d < TAPS; d++) {
-                        long long lin = (long long)(b2 + dk) * (long long)VV + (long long)(b1 + dj2) * V + (b0 + d);
-                        if (lin >= 0 && lin < V3) acc = fmaf(wi[d] * wj[dj2] * wk[dk], ld_f32(vol + lin), acc);
+                        const long long lin = (long long)(b2 + dk) * (long long)VV + (long long)(b1 + dj2) * V + (b0 + d);
+                        if (lin >= 0 && lin < V3) {
+                            const long long row = lin / V;
+                            acc = fmaf(wi[d] * wj[dj2] * wk[dk], ld_f32(vol + row * P + (lin - row * V)), acc);
+                        }
                     }
         }
         *out = acc * outScale;
     }
 }
 
-template <typename TV, int TAPS>
-static cudaError_t launch_fp_t(const TV *vol, float *img, const float *ker, const float *axes, int n,
+template <typename TV, int TAPS, bool VEC>
+static cudaError_t launch_fp_t(const TV *vol, int P, float *img, const float *ker, const float *axes, int n,
                                const Geom &g, const float *scale, cudaStream_t s)
 {
     const int tilesX = (g.M + kFpTile - 1) / kFpTile;
     const long long nItems = (long long)n * tilesX * tilesX;
     if (nItems == 0) return cudaSuccess;
     int perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fp_kernel<TV, TAPS>, kFpThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fp_kernel<TV, TAPS, VEC>, kFpThreads, 0);
     if (perSm <= 0) perSm = 1;
     long long grid = (long long)num_sms() * perSm;
     if (grid > nItems) grid = nItems;
-    fp_kernel<TV, TAPS><<<(unsigned)grid, kFpThreads, 0, s>>>(vol, g.V, img, g.M, axes, g.mask_radius, ker,
-                                                               g.ker_size, g.ker_hw, tilesX, nItems, scale);
+    fp_kernel<TV, TAPS, VEC><<<(unsigned)grid, kFpThreads, 0, s>>>(vol, g.V, P, img, g.M, axes, g.mask_radius, ker,
+                                                                    g.ker_size, g.ker_hw, tilesX, nItems, scale);
     count_launches(1);
     return cudaGetLastError();
 }
 
-cudaError_t launch_forward_project(const void *d_vol, int vprec, float *d_img, const float *d_ker,
+template <typename TV>
+static cudaError_t launch_fp_p(const void *d_vol, int P, float *d_img, const float *d_ker, const float *d_axes, int n,
+                               const Geom &g, bool five_taps, const float *scale, cudaStream_t s)
+{
+    const TV *v = (const TV *)d_vol;
+    if (five_taps) return launch_fp_t<TV, 5, false>(v, P, d_img, d_ker, d_axes, n, g, scale, s);
+    // 2-byte storage only: with FP32 the 8-element rows double the bytes each
+    // tap row moves through L1, which costs more than the loads it saves
+    const bool vec = sizeof(TV) == 2 && P % 8 == 0 && P >= g.V + 4 && ((size_t)d_vol & 15) == 0;
+    if (vec) return launch_fp_t<TV, 4, true>(v, P, d_img, d_ker, d_axes, n, g, scale, s);
+    return launch_fp_t<TV, 4, false>(v, P, d_img, d_ker, d_axes, n, g, scale, s);
+}
+
+cudaError_t launch_forward_project(const void *d_vol, int vprec, int pitch, float *d_img, const float *d_ker,
                                    const float *d_axes, int n, const Geom &g, bool five_taps, const float *scale,
                                    cudaStream_t s)
 {
-    if (vprec == kF32)
-        return five_taps ? launch_fp_t<float, 5>((const float *)d_vol, d_img, d_ker, d_axes, n, g, scale, s)
-                         : launch_fp_t<float, 4>((const float *)d_vol, d_img, d_ker, d_axes, n, g, scale, s);
-    if (vprec == kF16)
-        return five_taps ? launch_fp_t<__half, 5>((const __half *)d_vol, d_img, d_ker, d_axes, n, g, scale, s)
-                         : launch_fp_t<__half, 4>((const __half *)d_vol, d_img, d_ker, d_axes, n, g, scale, s);
-    return five_taps ? launch_fp_t<__nv_bfloat16, 5>((const __nv_bfloat16 *)d_vol, d_img, d_ker, d_axes, n, g, scale, s)
-                     : launch_fp_t<__nv_bfloat16, 4>((const __nv_bfloat16 *)d_vol, d_img, d_ker, d_axes, n, g, scale, s);
+    if (vprec == kF32) return launch_fp_p<float>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s);
+    if (vprec == kF16) return launch_fp_p<__half>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s);
+    return launch_fp_p<__nv_bfloat16>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s);
 }
 
 // ---------------------------------------------------------------------------

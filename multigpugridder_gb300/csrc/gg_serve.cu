@@ -248,7 +248,7 @@ void enqueue(gg_server *S, Request &r)
         const int b = std::min(B, r.n - c0);
         const cufftHandle p = lane_plan(L, r.op == GG_OP_FORWARD ? CUFFT_C2R : CUFFT_R2C, v.M, pow2ceil(b));
         if (r.op == GG_OP_FORWARD) {
-            GS_CK(launch_forward_project(v.cas, kF32, d_cas, v.ker, d_axes + (size_t)c0 * 9, b, v.g, v.five_taps,
+            GS_CK(launch_forward_project(v.cas, kF32, v.V, d_cas, v.ker, d_axes + (size_t)c0 * 9, b, v.g, v.five_taps,
                                          nullptr, s));
             GS_CK(launch_cas_images_to_spectrum(d_cas, v.M, b, d_spec, s));
             GS_CKF(cufftExecC2R(p, d_spec, d_real));
