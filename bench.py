@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--serve-lanes", type=int, default=8)
     ap.add_argument("--serve-closed", type=int, default=200,
                     help="requests in the closed-loop served vs sequential plain-path comparison")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 256^3 storage-precision comparison")
+    ap.add_argument("--no-autograd", action="store_true", help="skip the gradient-descent timing")
     return ap.parse_args()
 
 
@@ -62,7 +64,7 @@ def workload(args):
     from multigpugridder_gb300 import synthetic
 
     N = args.size
-    n_blobs = 100 if N == 128 else max(10, N // 2)
+    n_blobs = {64: 20, 128: 100, 256: 400}.get(N, max(10, N // 2))
     vol = synthetic.blob_volume(N, n_blobs, seed=2)
     side = int(round(args.directions ** 0.5))
     if side * side == args.directions:
@@ -273,9 +275,15 @@ def run_gb300(args):
     except (OSError, ValueError):
         pass
     peak = peaks.get("hbm_gbs") or 6800.0
+    # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
+    # the dominant kernel, the mean over the 10 launches of a one-pass ncu
+    # capture of this workload at full size; null for other shapes
+    traffic = None
+    if dom == "back" and fused and N == 128 and args.batch == 2000 and args.precision == "f32" and n == 10000:
+        traffic = 2.07e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": "measured" if peaks.get("hbm_gbs") else "fallback",
-                "traffic": None, "bytes_per_unit": bpu[dom], "units_per_launch": units_per_launch,
+                "traffic": traffic, "bytes_per_unit": bpu[dom], "units_per_launch": units_per_launch,
                 "kernel_ms": {k: v[0] / args.steps for k, v in prof.items()}}
 
     e2e = None
@@ -289,9 +297,13 @@ def run_gb300(args):
                 "sample": "%d of %d directions timed, step extrapolated (t_fixed + D/S * t_sample)" % (S, n)}
 
     g.close()
-    serve = None
+    serve = prec = grad = None
     if rank == 0 and world == 1 and args.serve_seconds > 0:
         serve = run_serve(args)
+    if rank == 0 and world == 1 and not args.no_precision and args.size == 128:
+        prec = run_precision(args)
+    if rank == 0 and world == 1 and not args.no_autograd and args.size == 128:
+        grad = run_autograd(args)
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -304,7 +316,7 @@ def run_gb300(args):
                           "l2": "inputs larger than L2 (10,000 images = %d MB per step) and an untimed %d MB "
                                 "write between steps" % (n * N * N * 4 >> 20, flush.numel() * 4 >> 20)},
                "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
-               "clocks": clk, "step_ms": ms_steps, "serve": serve}
+               "clocks": clk, "step_ms": ms_steps, "serve": serve, "precision": prec, "autograd": grad}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -444,6 +456,124 @@ def run_serve(args):
             "lanes": args.serve_lanes, "offered": res_offered, "at_70pct_capacity": res_70,
             "closed_loop": {"requests": len(closed), "served_rps": served_closed, "sequential_plain_rps": seq_closed,
                             "speedup": served_closed / seq_closed}}
+
+
+# ---- storage precision at 256^3 ------------------------------------------------
+def run_precision(args):
+    """256^3 Gaussian-blob volume (400 blobs), interpFactor 2 (CAS volume 518^3),
+    5,000 random-quaternion directions: setVolume + forwardProject +
+    reconstructVol with FP32, BF16 and FP16 storage (FP32 accumulation).
+    Reports pairs/s per storage type and the relative L2 of the images and the
+    reconstruction against the FP32 path (the FP64 oracle comparison runs in
+    tests/test_gpu_precision.py at sizes the CPU finishes)."""
+    import torch
+
+    import multigpugridder_gb300 as gg
+    from multigpugridder_gb300 import synthetic
+    from multigpugridder_gb300._lib import check, lib
+
+    L = lib()
+    N, n = 256, 5000
+    vol = synthetic.blob_volume(N, 400, seed=3)
+    axes = synthetic.quaternion_axes(n, seed=3).astype(np.float32)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d_vol = torch.from_numpy(vol).to(dev)
+    d_axes = torch.from_numpy(axes).to(dev)
+    stream = torch.cuda.Stream(device=dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    out, ref = {}, {}
+
+    def vp(t):
+        return ctypes.c_void_p(t.data_ptr())
+
+    for prec in ("f32", "bf16", "f16"):
+        g = gg.MultiGPUGridder(N, n, 2.0, MaxAxesToAllocate=1000, precision=prec)
+        h = g.handle
+        imgs = torch.empty((n, N, N), dtype=torch.float32, device=dev)
+        rec = torch.empty((N, N, N), dtype=torch.float32, device=dev)
+
+        def step():
+            check(L.gg_set_volume_dev(h, vp(d_vol), sp), h)
+            check(L.gg_forward_project_dev(h, vp(d_axes), n, vp(imgs), None, sp), h)
+            check(L.gg_reconstruct_volume_dev(h, vp(d_axes), n, vp(imgs), vp(rec), sp), h)
+
+        with torch.cuda.stream(stream):
+            step()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        res = {"pairs_per_s": n / (ms / 1e3), "ms_per_step": ms}
+        if prec == "f32":
+            ref = {"images": imgs.clone(), "rec": rec.clone()}
+        else:
+            for k, t in (("images", imgs), ("rec", rec)):
+                res["rel_l2_%s_vs_f32" % k] = float(torch.linalg.vector_norm((t - ref[k]).double())
+                                                    / torch.linalg.vector_norm(ref[k].double()))
+        out[prec] = res
+        g.close()
+        del imgs, rec
+    return {"workload": "256^3 volume (400 blobs), interpFactor 2 (CAS volume 518^3), 5,000 random-quaternion "
+                        "directions: setVolume + forwardProject + reconstructVol, storage f32/bf16/f16, FP32 "
+                        "accumulation", "results": out}
+
+
+# ---- differentiation -----------------------------------------------------------
+def run_autograd(args):
+    """torch FP32 volume 128^3 (requires_grad, Gaussian-blob init), interpFactor
+    2, batches of 4,096 random directions, loss ||P(V) - Y||^2 with
+    Y = P(V_true) + Gaussian noise at SNR 0.1, backward through the exact
+    adjoint; 20 gradient-descent iterations timed."""
+    import torch
+
+    from multigpugridder_gb300 import synthetic
+    from multigpugridder_gb300.autograd import ForwardProjector
+
+    N, B, iters = 128, 4096, 20
+    dev = torch.device("cuda", torch.cuda.current_device())
+    proj = ForwardProjector(N, 2.0, max_batch=B)
+    v_true = torch.from_numpy(synthetic.blob_volume(N, 100, seed=4)).to(dev)
+    batches = []
+    for k in range(4):
+        ax = torch.from_numpy(synthetic.quaternion_axes(B, seed=40 + k).astype(np.float32)).to(dev)
+        with torch.no_grad():
+            clean = proj.project(v_true, ax)
+            sigma = float(torch.sqrt(clean.var() / 0.1))
+            gen = torch.Generator(device=dev).manual_seed(400 + k)
+            y = clean + sigma * torch.randn(clean.shape, device=dev, generator=gen)
+        batches.append((ax, y))
+    vol = torch.from_numpy(synthetic.blob_volume(N, 100, seed=41)).to(dev).requires_grad_(True)
+    lr = 1e-9
+
+    def it(k):
+        ax, y = batches[k % len(batches)]
+        loss = torch.sum((proj.project(vol, ax) - y) ** 2)
+        loss.backward()
+        with torch.no_grad():
+            vol.sub_(lr * vol.grad)
+            vol.grad = None
+        return loss.detach()
+
+    for k in range(2):
+        it(k)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    losses = []
+    a.record()
+    for k in range(iters):
+        losses.append(it(k))
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / iters
+    proj.close()
+    first = [float(x) for x in losses[:4]]
+    last = [float(x) for x in losses[-4:]]
+    return {"workload": "128^3 FP32 volume, interpFactor 2, batches of 4,096 random directions, loss "
+                        "||P(V) - Y||^2 (Y = P(V_true) + noise at SNR 0.1), 20 gradient-descent iterations",
+            "ms_per_iteration": ms, "directions_per_s": B / (ms / 1e3),
+            "loss_first_cycle": sum(first), "loss_last_cycle": sum(last)}
 
 
 def run_e2e(args, g, vol, axes, world):

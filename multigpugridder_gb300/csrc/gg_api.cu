@@ -1,8 +1,8 @@
 // Host engine and C ABI of the GB300 gridder (include/gg_gridder.h).
 //
-// One handle owns one GPU's state: the resident FP32 CAS volume (plus the
-// copy the forward projection reads: rows padded for aligned vector loads, in
-// the selected storage precision), the KB table and pre-compensation vector, batch buffers and
+// One handle owns one GPU's state: the resident FP32 CAS volume (plus, with
+// FP16/BF16 storage, the copy the forward projection reads: rows padded for
+// aligned vector loads), the KB table and pre-compensation vector, batch buffers and
 // cached cuFFT plans.  It replaces the reference's MultiGPUGridder /
 // gpuGridder / AbstractGridder trio (src/Gridders/) for one device:
 //   * the volume is prepared on the device once per setVolume instead of on
@@ -148,8 +148,8 @@ struct gg_gridder {
     DevBuf<float> ker;
     DevBuf<double> precomp;
     DevBuf<float> cas;       // FP32 CAS volume V^3 (resident)
-    DevBuf<float> cas_fp;    // the CAS volume as the forward projection reads it: row pitch
-                             // fp_pitch(V), storage `prec` (FP16 scaled by scales[0])
+    DevBuf<float> cas_fp;    // FP16/BF16 copy the forward projection reads: row pitch
+                             // fp_pitch(V) (FP16 scaled by scales[0])
     bool cas_fp_valid = false;
     DevBuf<float> pd;        // plane density V^3
     DevBuf<float> adj;       // CAS-volume gradient V^3 (forward-operator adjoint)
@@ -301,7 +301,8 @@ void check_axes_count(int n)
 // rows, storage precision).
 void update_fp(gg_gridder *h, cudaStream_t s)
 {
-    if (h->cas_fp_valid) return;
+    // FP32 taps are read one by one from the dense volume itself
+    if (h->prec == kF32 || h->cas_fp_valid) return;
     const size_t V3 = (size_t)h->V * h->V * h->V;
     const int P = fp_pitch(h->V);
     h->cas_fp.ensure(((size_t)P * h->V * h->V * prec_bytes(h->prec) + 3) / 4);
@@ -345,8 +346,9 @@ void fp_batch(gg_gridder *h, const float *d_axes, int b, float *cas_out, float *
 {
     auto &S = h->slot[sl];
     ProfScope ps(h, s, GG_KERNEL_FORWARD);
-    GG_CK(launch_forward_project(h->cas_fp.p, h->prec, fp_pitch(h->V), cas_out, h->ker.p, d_axes, b, h->geom(),
-                                 h->five_taps, h->vol_scale(), s));
+    const bool dense = h->prec == kF32;
+    GG_CK(launch_forward_project(dense ? h->cas.p : h->cas_fp.p, h->prec, dense ? h->V : fp_pitch(h->V), cas_out,
+                                 h->ker.p, d_axes, b, h->geom(), h->five_taps, h->vol_scale(), s));
     ps.done();
     if (img_out) {
         GG_CK(launch_cas_images_to_spectrum(cas_out, h->M, b, S.spec.p, s));
