@@ -106,3 +106,38 @@ def test_synthetic_inputs_match_the_oracle_generators():
     assert np.array_equal(synthetic.blob_volume(24, 10, seed=5), O.blob_volume(24, 10, seed=5))
     assert np.array_equal(synthetic.quaternion_axes(64, 6).astype(np.float32), O.quaternion_axes(64, 6).astype(np.float32))
     assert np.array_equal(synthetic.grid_axes(12, 10).astype(np.float32), O.grid_axes(12, 10).astype(np.float32))
+
+
+def test_compat_header_names_are_exported(L):
+    """include/gg_compat.h: the C names the reference's Python ctypes class
+    binds (MultiGPUGridder_Python.py:11-48) are exported, and the header is
+    valid C."""
+    import re
+
+    path = os.path.join(ROOT, "include", "gg_compat.h")
+    txt = re.sub(r"/\*.*?\*/", "", open(path).read(), flags=re.S)
+    names = sorted(set(re.findall(r"\b([A-Z][A-Za-z_]+)\s*\(", txt)))
+    want = {"Gridder_new", "SetNumberGPUs", "SetNumberStreams", "SetVolume", "GetVolume", "ResetVolume", "SetImages",
+            "GetImages", "SetAxes", "SetImgSize", "SetMaskRadius", "Forward_Project", "Back_Project"}
+    assert want <= set(names)
+    missing = [s for s in names if not hasattr(L, s)]
+    assert not missing, missing
+    cc = shutil.which("gcc")
+    if cc:
+        subprocess.run([cc, "-Wall", "-Werror", "-fsyntax-only", "-x", "c", path], check=True)
+
+
+def test_compat_errors_without_a_volume(L):
+    """The old API has no status: a call made too early leaves a message in
+    gg_global_error() and touches nothing (no GPU work is reached)."""
+    L.Gridder_new.restype = ctypes.c_void_p
+    L.Forward_Project.argtypes = [ctypes.c_void_p]
+    L.Forward_Project.restype = ctypes.c_void_p
+    L.Gridder_delete.argtypes = [ctypes.c_void_p]
+    L.GetImages.argtypes = [ctypes.c_void_p]
+    L.GetImages.restype = ctypes.POINTER(ctypes.c_float)
+    g = L.Gridder_new()
+    L.Forward_Project(g)
+    assert b"SetVolume" in L.gg_global_error()
+    assert not L.GetImages(g)
+    L.Gridder_delete(g)
