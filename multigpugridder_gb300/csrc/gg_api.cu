@@ -398,7 +398,7 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
     if (ones) iprec = kF32;
     ProfScope ps(h, s, ones ? GG_KERNEL_DENSITY : GG_KERNEL_BACK);
     if (h->bp_mode == GG_BP_ADJOINT && !ones) {
-        GG_CK(launch_back_project_adjoint(target, src, iprec, h->ker.p, d_axes, b, h->geom(), scale, s));
+        GG_CK(launch_back_project_adjoint(target, src, iprec, h->ker.p, d_axes, b, h->geom(), scale, !h->five_taps, s));
     } else if (pd && !ones) {
         GG_CK(launch_back_project_ref_density(target, pd, src, iprec, h->ker.p, d_axes, b, h->geom(), scale, s));
         pd = nullptr;
@@ -411,7 +411,7 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
         const size_t MM = (size_t)h->M * h->M;
         ProfScope pd_ps(h, s, GG_KERNEL_DENSITY);
         GG_CK(launch_fill(S.casimg.p, MM * b, 1.0f, s));
-        GG_CK(launch_back_project_adjoint(pd, S.casimg.p, kF32, h->ker.p, d_axes, b, h->geom(), nullptr, s));
+        GG_CK(launch_back_project_adjoint(pd, S.casimg.p, kF32, h->ker.p, d_axes, b, h->geom(), nullptr, !h->five_taps, s));
         pd_ps.done();
     }
 }
@@ -435,7 +435,7 @@ void forward_adjoint(gg_gridder *h, const float *d_axes, int n, const float *d_i
         GG_CK(launch_spectrum_to_cas_images_adjoint(S.spec.p, h->M, b, S.casimg.p, s));
         ProfScope ps(h, s, GG_KERNEL_BACK);
         GG_CK(launch_back_project_adjoint(h->adj.p, S.casimg.p, kF32, h->ker.p, d_axes + (size_t)a0 * 9, b, h->geom(),
-                                          nullptr, s));
+                                          nullptr, !h->five_taps, s));
         ps.done();
     }
     const size_t M3 = (size_t)h->M * h->M * h->M;
@@ -1182,8 +1182,9 @@ extern "C" int gg_back_project_adjoint_kernel(float *d_cas_volume, const float *
         return GG_ERR_INVALID_ARG;
     }
     Geom g{cas_vol_size, cas_img_size, mask_radius, kb_table_size, ker_hwidth};
+    // zero table edges were checked above
     cudaError_t e = launch_back_project_adjoint(d_cas_volume, d_cas_images, kF32, d_kb_table, d_axes, n_axes, g, nullptr,
-                                                (cudaStream_t)stream);
+                                                true, (cudaStream_t)stream);
     if (e != cudaSuccess) {
         g_global_err = cudaGetErrorString(e);
         return GG_ERR_CUDA;

@@ -57,10 +57,12 @@ cudaError_t launch_back_project_ref_density(float *d_vol, float *d_pd, const voi
                                             const float *d_ker, const float *d_axes, int n, const Geom &g,
                                             const float *d_scale, cudaStream_t s);
 
-// Exact adjoint of launch_forward_project, accumulated into d_vol.
+// Exact adjoint of launch_forward_project (4 taps), accumulated into d_vol.
+// zero_edges: the KB table's first and last entries are 0 (the fast path
+// relies on it).
 cudaError_t launch_back_project_adjoint(float *d_vol, const void *d_img, int iprec, const float *d_ker,
                                         const float *d_axes, int n, const Geom &g, const float *d_scale,
-                                        cudaStream_t s);
+                                        bool zero_edges, cudaStream_t s);
 
 // ---- CAS / FFT stages (gg_cas.cu) ------------------------------------------
 // Volume N^3 -> real M^3 FFT input: centred zero-pad, separable precomp

@@ -283,21 +283,11 @@ cudaError_t launch_forward_project(const void *d_vol, int vprec, int pitch, floa
 }
 
 // ---------------------------------------------------------------------------
-// Back projection, reference window rule
+// Back projection: the reference window and shared constants
 // ---------------------------------------------------------------------------
-// One CTA owns an 8x8x4 brick of voxels (one voxel per thread) and keeps each
-// voxel's sum in a register, so the volume is written once per launch with a
-// coalesced read-modify-write and no atomics.  Directions are staged through
-// shared memory in chunks; a chunk is first culled against the brick (slab
-// |dot(v - c, z)| <= kerHWidth must reach the brick), then each warp culls
-// against its own 8x4x1 sub-brick, and only then does each voxel apply the
-// reference's per-voxel test and 5x5 window (gpuBackProject.cu:54-107).
-// Directions are visited in order, so each voxel sums its directions in the
-// same order as the reference.
-constexpr int kBpBX = 8, kBpBY = 8, kBpBZ = 4;
-constexpr int kBpThreads = kBpBX * kBpBY * kBpBZ;
+// Directions are staged through shared memory in chunks of kBpChunk, one per
+// thread of a CTA for the cull.
 constexpr int kBpChunk = 256;
-static_assert(kBpChunk == kBpThreads, "the cull compaction gives one direction per thread");
 
 // Conservative reach of the slab test: fp32 rounding of f_imgk is far below this.
 constexpr float kCullEps = 1e-2f;
@@ -353,169 +343,6 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
     }
 }
 
-// DENS: also accumulate the plane density -- the back projection of
-// all-ones CAS images over the same directions (reconstructVol,
-// MultiGPUGridder_Matlab_Class.m:300-304) -- into `pd`.  Both sums use the
-// same weights, so one pass does the work of the reference's two.
-template <typename TI, bool ONES, bool ADJ, bool DENS>
-__global__ void __launch_bounds__(kBpThreads)
-bp_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
-          const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
-          float kerHW, int bricksX, int bricksY, const float *__restrict__ d_scale)
-{
-    __shared__ float sker[kMaxKerSize];
-    __shared__ float sax[kBpChunk * 9];
-    __shared__ int slist[kBpChunk];
-    __shared__ int swarp[kBpChunk / 32];
-    __shared__ int scount;
-
-    const int tid = threadIdx.x;
-    const int bxi = blockIdx.x % bricksX;
-    const int byi = (blockIdx.x / bricksX) % bricksY;
-    const int bzi = blockIdx.x / (bricksX * bricksY);
-    const int x0 = bxi * kBpBX, y0 = byi * kBpBY, z0 = bzi * kBpBZ;
-    // each warp owns a compact 4x4x2 block of the brick: a small extent along
-    // any projection direction, so fewer lanes sit outside the slab when the
-    // warp is inside it
-    const int warp = tid >> 5, lane = tid & 31;
-    const int wx = (warp & 1) * 4, wy = ((warp >> 1) & 1) * 4, wz = (warp >> 2) * 2;
-    const int vi = x0 + wx + (lane & 3);
-    const int vj = y0 + wy + ((lane >> 2) & 3);
-    const int vk = z0 + wz + (lane >> 4);
-    const int volCenter = (int)((float)V) / 2;
-    const int imgCenter = (int)((float)M) / 2;
-
-    // Skip bricks that lie entirely outside the mask sphere.
-    {
-        const float cx = fmaxf(fabsf((float)(x0 + (kBpBX - 1) * 0.5f - volCenter)) - 0.5f * (kBpBX - 1), 0.f);
-        const float cy = fmaxf(fabsf((float)(y0 + (kBpBY - 1) * 0.5f - volCenter)) - 0.5f * (kBpBY - 1), 0.f);
-        const float cz = fmaxf(fabsf((float)(z0 + (kBpBZ - 1) * 0.5f - volCenter)) - 0.5f * (kBpBZ - 1), 0.f);
-        // the adjoint also reaches voxels up to 2*sqrt(3) beyond the mask sphere
-        const float reach = ADJ ? (float)maskR + 4.0f : (float)maskR;
-        if (cx * cx + cy * cy + cz * cz > reach * reach + 1.0f) return;
-    }
-
-    load_table(sker, ker, kerSize);
-
-    const long long d2 = (long long)(vi - volCenter) * (vi - volCenter) + (long long)(vj - volCenter) * (vj - volCenter) +
-                         (long long)(vk - volCenter) * (vk - volCenter);
-    const bool active = vi < V && vj < V && vk < V && (ADJ || d2 <= (long long)maskR * maskR);
-
-    const int convW = (int)roundf(kerHW);
-    const float kerCenter = ((float)kerSize - 1) / 2;
-    const float kerScale = kerCenter / kerHW;
-    const float kerCenterHalf = kerCenter + 0.5f;
-    // reach of the brick / warp sub-brick along the projection direction
-    const float bcx = x0 + 0.5f * (kBpBX - 1) - volCenter, bcy = y0 + 0.5f * (kBpBY - 1) - volCenter,
-                bcz = z0 + 0.5f * (kBpBZ - 1) - volCenter;
-    const float wcx = x0 + wx + 1.5f - volCenter, wcy = y0 + wy + 1.5f - volCenter, wcz = z0 + wz + 0.5f - volCenter;
-    // slab half-thickness: kerHW for the reference rule; for the adjoint, any
-    // voxel within the 4^3 window of a sample point (|r| < 2 per axis)
-    const float slab = ADJ ? 2.0f * 1.7320508f + kCullEps : kerHW + kCullEps;
-    const int MM = M * M;
-
-    float accAll = 0.0f, accW = 0.0f;
-    for (int c0 = 0; c0 < n; c0 += kBpChunk) {
-        const int cn = min(kBpChunk, n - c0);
-        __syncthreads();
-        for (int t = tid; t < cn * 9; t += kBpThreads) sax[t] = __ldg(axes + (size_t)c0 * 9 + t);
-        __syncthreads();
-        // brick-level cull, compacted in direction order
-        bool keep = false;
-        if (tid < cn) {
-            const float *ax = sax + tid * 9;
-            const float zx = ax[6], zy = ax[7], zz = ax[8];
-            const float d = bcx * zx + bcy * zy + bcz * zz;
-            const float ext = 0.5f * ((kBpBX - 1) * fabsf(zx) + (kBpBY - 1) * fabsf(zy) + (kBpBZ - 1) * fabsf(zz));
-            keep = fabsf(d) <= slab + ext;
-        }
-        const unsigned ballot = __ballot_sync(0xffffffffu, keep);
-        if ((tid & 31) == 0 && tid < kBpChunk) swarp[tid >> 5] = __popc(ballot);
-        __syncthreads();
-        if (tid < kBpChunk) {
-            int off = 0;
-            for (int w = 0; w < (tid >> 5); w++) off += swarp[w];
-            if (keep) slist[off + __popc(ballot & ((1u << (tid & 31)) - 1u))] = tid;
-            if (tid == kBpChunk - 1) {
-                int tot = 0;
-                for (int w = 0; w < kBpChunk / 32; w++) tot += swarp[w];
-                scount = tot;
-            }
-        }
-        __syncthreads();
-        const int count = scount;
-
-        for (int q = 0; q < count; q++) {
-            const int al = slist[q];
-            const float *ax = sax + al * 9;
-            const float nx0 = ax[0], nx1 = ax[1], nx2 = ax[2];
-            const float ny0 = ax[3], ny1 = ax[4], ny2 = ax[5];
-            const float nz0 = ax[6], nz1 = ax[7], nz2 = ax[8];
-            {   // warp-level cull (uniform across the warp): the warp's 4x4x2 block
-                const float d = wcx * nz0 + wcy * nz1 + wcz * nz2;
-                const float ext = 0.5f * (3.0f * fabsf(nz0) + 3.0f * fabsf(nz1) + fabsf(nz2));
-                if (fabsf(d) > slab + ext) continue;
-            }
-            if (!active) continue;
-            const TI *img_ptr = img + (size_t)(c0 + al) * MM;
-            if (!ADJ) {
-                // gpuBackProject.cu:62-107
-                const float a0 = (float)vi - volCenter, a1 = (float)vj - volCenter, a2 = (float)vk - volCenter;
-                const float f_imgi = __fadd_rn(voxel_proj(a0, a1, a2, nx0, nx1, nx2), (float)imgCenter);
-                const float f_imgj = __fadd_rn(voxel_proj(a0, a1, a2, ny0, ny1, ny2), (float)imgCenter);
-                const float f_imgk = voxel_proj(a0, a1, a2, nz0, nz1, nz2);
-                if (!(fabsf(f_imgk) <= kerHW)) continue;
-                const int imgi = (int)roundf(f_imgi);
-                const int imgj = (int)roundf(f_imgj);
-                float cumSum = 0.0f, cumW = 0.0f;
-                const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk, (float)volCenter,
-                                   kerScale, kerCenter + 0.5f};
-                if (imgi >= 2 && imgj >= 2 && imgi + 2 < M && imgj + 2 < M)
-                    ref_window<TI, ONES, DENS, true>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cumSum, cumW);
-                else
-                    ref_window<TI, ONES, DENS, false>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cumSum, cumW);
-                accAll += cumSum;
-                if (DENS) accW += cumW;
-            } else {
-                // Exact adjoint of fp_kernel<., 4>: every pixel whose 4^3
-                // window contains this voxel, with the forward weight.  Such a
-                // pixel lies within 2*sqrt(3) of the voxel's projection.
-                const float pi = ((float)vi - volCenter) * nx0 + ((float)vj - volCenter) * nx1 + ((float)vk - volCenter) * nx2;
-                const float pj = ((float)vi - volCenter) * ny0 + ((float)vj - volCenter) * ny1 + ((float)vk - volCenter) * ny2;
-                const float pk = ((float)vi - volCenter) * nz0 + ((float)vj - volCenter) * nz1 + ((float)vk - volCenter) * nz2;
-                if (!(fabsf(pk) < 2.0f * 1.7320508f + kCullEps)) continue;
-                const int ilo = (int)ceilf(pi - 3.47f), ihi = (int)floorf(pi + 3.47f);
-                const int jlo = (int)ceilf(pj - 3.47f), jhi = (int)floorf(pj + 3.47f);
-                const long long R2 = (long long)maskR * maskR;
-                float s = 0.0f;
-                for (int dj = jlo; dj <= jhi; dj++) {
-                    for (int di = ilo; di <= ihi; di++) {
-                        if ((long long)di * di + (long long)dj * dj > R2) continue;
-                        const int pxi = di + imgCenter, pxj = dj + imgCenter;
-                        if (pxi < 0 || pxi >= M || pxj < 0 || pxj >= M) continue;
-                        const float fi = sample_coord(nx0, ny0, di, dj, volCenter);
-                        const float fj = sample_coord(nx1, ny1, di, dj, volCenter);
-                        const float fk = sample_coord(nx2, ny2, di, dj, volCenter);
-                        // membership in the forward window floor(f)-1 .. floor(f)+2
-                        const int oi = vi - ((int)floorf(fi) - 1), oj = vj - ((int)floorf(fj) - 1), ok = vk - ((int)floorf(fk) - 1);
-                        if ((unsigned)oi > 3u || (unsigned)oj > 3u || (unsigned)ok > 3u) continue;
-                        const float w = kb_weight(sker, (float)vi - fi, kerScale, kerCenterHalf, kerSize) *
-                                        kb_weight(sker, (float)vj - fj, kerScale, kerCenterHalf, kerSize) *
-                                        kb_weight(sker, (float)vk - fk, kerScale, kerCenterHalf, kerSize);
-                        s = fmaf(w, ld_f32(img_ptr + (size_t)pxj * M + pxi), s);
-                    }
-                }
-                accAll += s;
-            }
-        }
-    }
-    if (active) {
-        const size_t o = (size_t)vk * V * V + (size_t)vj * V + vi;
-        vol[o] = vol[o] + accAll * (d_scale ? *d_scale : 1.0f);
-        if (DENS) pd[o] = pd[o] + accW;
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Back projection, reference window rule
 // ---------------------------------------------------------------------------
@@ -529,6 +356,7 @@ bp_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__re
 // the per-voxel sums are those of the reference kernel's loops, bit for bit.
 constexpr int kCBX = 16, kCBY = 8, kCBZ = 8; // brick: 2x2x2 warp blocks of 8x4x4
 constexpr int kCThreads = 256;
+static_assert(kBpChunk == kCThreads, "the cull compaction gives one direction per thread");
 constexpr int kWarpVox = 128;                // voxels per warp block
 
 // The fast window.  For a voxel coordinate v and a window pixel whose
@@ -548,7 +376,7 @@ constexpr int kWarpVox = 128;                // voxels per warp block
 // window of the warp's block can touch, staged per direction with the
 // reference's linear-index rule (a pixel whose index falls outside the image
 // reads as zero), so the windows read them at constant offsets.
-constexpr int kFootW = 16, kFootH = 16, kFootS = 17; // footprint, row stride
+constexpr int kFootW = 16; // reference-rule footprint width (the adjoint's is 24)
 constexpr int kTabRep = 1;                           // interleaved table copies
 
 __device__ __forceinline__ float lds_f32(unsigned addr)
@@ -565,19 +393,19 @@ struct FootWin {
     float c0, c1, c2; // h - v*s per axis
 };
 
-// One voxel's 5x5 window from the footprint (fbase = its top-left pixel);
-// table entry floor(x) is read at tab + bits(x + 1.5*2^23) * 4 * kTabRep.
-// Sums in the reference's order.
-template <bool DENS>
+// One voxel's W x W window from the footprint (fbase = its top-left pixel,
+// rows FS apart); table entry floor(x) is read at
+// tab + bits(x + 1.5*2^23) * 4 * kTabRep.  Sums row by row, as the reference.
+template <bool DENS, int W, int FS>
 __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase, unsigned tab, float pi0, float pj0,
                                             float &cumSum, float &cumW)
 {
 #pragma unroll
-    for (int jo = 0; jo < 5; jo++) {
+    for (int jo = 0; jo < W; jo++) {
         const float pj = pj0 + (float)jo;
         const float py0 = __fmul_rn(pj, q.ny0), py1 = __fmul_rn(pj, q.ny1), py2 = __fmul_rn(pj, q.ny2);
 #pragma unroll
-        for (int io = 0; io < 5; io++) {
+        for (int io = 0; io < W; io++) {
             const float pi = pi0 + (float)io;
             const float q0 = __fadd_rn(__fmaf_rn(pi, q.nx0, py0), q.vc);
             const float q1 = __fadd_rn(__fmaf_rn(pi, q.nx1, py1), q.vc);
@@ -588,22 +416,73 @@ __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase
             float w = lds_f32(tab + b0 * (4u * kTabRep));
             w = __fmul_rn(w, lds_f32(tab + b1 * (4u * kTabRep)));
             w = __fmul_rn(w, lds_f32(tab + b2 * (4u * kTabRep)));
-            cumSum = __fmaf_rn(fbase[jo * kFootS + io], w, cumSum);
+            cumSum = __fmaf_rn(fbase[jo * FS + io], w, cumSum);
             if (DENS) cumW = __fadd_rn(cumW, w);
         }
     }
 }
 
 // Table entries below and above the table a window can reach with
-// orthonormal axes: |Q - v| <= sqrt(2.5^2 + 2.5^2 + 2^2) < 4.1 per axis.
-static inline int bp_table_pad(int kerSize) { return (int)ceil(4.25 * (kerSize - 1) / 4.0) + 2; }
+// orthonormal axes: |Q - v| <= sqrt(2.5^2 + 2.5^2 + 2^2) < 4.1 per axis for
+// the reference window, sqrt(3.5^2 + 3.5^2 + 3.47^2) < 6.1 for the adjoint's.
+static inline int bp_table_pad(int kerSize, bool adj)
+{
+    return (int)ceil((adj ? 6.25 : 4.25) * (kerSize - 1) / 4.0) + 2;
+}
 
-template <typename TI, bool ONES, bool DENS>
+// The exact adjoint of fp_kernel<., 4> for one voxel, without the fast
+// path's assumptions: every in-mask pixel whose 4^3 forward window contains
+// the voxel, with the forward weight.  Such a pixel lies within 2*sqrt(3) of
+// the voxel's projection.
+template <typename TI>
+__device__ float adjoint_window_slow(int vi, int vj, int vk, int volCenter, float nx0, float nx1, float nx2, float ny0,
+                                     float ny1, float ny2, const TI *__restrict__ img_ptr, int M, int imgCenter,
+                                     int maskR, const float *sker, float kerScale, float kerCenterHalf, int kerSize)
+{
+    const float pi = ((float)vi - volCenter) * nx0 + ((float)vj - volCenter) * nx1 + ((float)vk - volCenter) * nx2;
+    const float pj = ((float)vi - volCenter) * ny0 + ((float)vj - volCenter) * ny1 + ((float)vk - volCenter) * ny2;
+    const int ilo = (int)ceilf(pi - 3.47f), ihi = (int)floorf(pi + 3.47f);
+    const int jlo = (int)ceilf(pj - 3.47f), jhi = (int)floorf(pj + 3.47f);
+    const long long R2 = (long long)maskR * maskR;
+    float s = 0.0f;
+    for (int dj = jlo; dj <= jhi; dj++) {
+        for (int di = ilo; di <= ihi; di++) {
+            if ((long long)di * di + (long long)dj * dj > R2) continue;
+            const int pxi = di + imgCenter, pxj = dj + imgCenter;
+            if (pxi < 0 || pxi >= M || pxj < 0 || pxj >= M) continue;
+            const float fi = sample_coord(nx0, ny0, di, dj, volCenter);
+            const float fj = sample_coord(nx1, ny1, di, dj, volCenter);
+            const float fk = sample_coord(nx2, ny2, di, dj, volCenter);
+            // membership in the forward window floor(f)-1 .. floor(f)+2
+            const int oi = vi - ((int)floorf(fi) - 1), oj = vj - ((int)floorf(fj) - 1), ok = vk - ((int)floorf(fk) - 1);
+            if ((unsigned)oi > 3u || (unsigned)oj > 3u || (unsigned)ok > 3u) continue;
+            const float w = kb_weight(sker, (float)vi - fi, kerScale, kerCenterHalf, kerSize) *
+                            kb_weight(sker, (float)vj - fj, kerScale, kerCenterHalf, kerSize) *
+                            kb_weight(sker, (float)vk - fk, kerScale, kerCenterHalf, kerSize);
+            s = fmaf(w, ld_f32(img_ptr + (size_t)pxj * M + pxi), s);
+        }
+    }
+    return s;
+}
+
+// ADJ: the exact adjoint of fp_kernel<., 4> (gradient of the forward
+// projection) instead of the reference rule.  The same pixel positions and
+// table indices (sample_coord is the reference's pixel-position expression),
+// a 7x7 window around the voxel's projection for voxels within 2*sqrt(3) of
+// the plane, pixels outside the image or the mask staged as zero, and the
+// index of r = v - Q: floor(fma(Q, -s, h + v*s)).  With a zero-edge table
+// every pixel whose forward window misses the voxel gets weight 0, so the
+// wider window adds exact zeros (zero_edges; otherwise the slow path checks
+// window membership as the forward does).
+template <typename TI, bool ONES, bool DENS, bool ADJ>
 __global__ void __launch_bounds__(kCThreads, 3)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
-                      float kerHW, int bricksX, int bricksY, int tabPad, const float *__restrict__ d_scale)
+                      float kerHW, int bricksX, int bricksY, int tabPad, int zeroEdges,
+                      const float *__restrict__ d_scale)
 {
+    constexpr int W = ADJ ? 7 : 5, HALF = W / 2;
+    constexpr int FW = ADJ ? 24 : kFootW, FH = FW, FS = FW + 1;
     extern __shared__ float stab[]; // (kerSize + 2 tabPad) entries x kTabRep copies
     __shared__ float sax[kBpChunk * 9];
     __shared__ int slist[kBpChunk];
@@ -613,7 +492,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     // lane per direction, directions in order, so no atomics are needed
     __shared__ float sacc[kCThreads / 32 * kWarpVox];
     __shared__ float saccw[DENS ? kCThreads / 32 * kWarpVox : 1];
-    __shared__ float sfoot[kCThreads / 32 * kFootH * kFootS];
+    __shared__ float sfoot[kCThreads / 32 * FH * FS];
     __shared__ unsigned char svox[kCThreads / 32 * kWarpVox];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -628,14 +507,16 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         const float cx = fmaxf(fabsf(x0 + 0.5f * (kCBX - 1) - volCenter) - 0.5f * (kCBX - 1), 0.f);
         const float cy = fmaxf(fabsf(y0 + 0.5f * (kCBY - 1) - volCenter) - 0.5f * (kCBY - 1), 0.f);
         const float cz = fmaxf(fabsf(z0 + 0.5f * (kCBZ - 1) - volCenter) - 0.5f * (kCBZ - 1), 0.f);
-        if (cx * cx + cy * cy + cz * cz > (float)maskR * (float)maskR + 1.0f) return;
+        // the adjoint also reaches voxels up to 2*sqrt(3) beyond the mask sphere
+        const float reach = ADJ ? (float)maskR + 4.0f : (float)maskR;
+        if (cx * cx + cy * cy + cz * cz > reach * reach + 1.0f) return;
     }
     for (int t = tid; t < (kerSize + 2 * tabPad) * kTabRep; t += kCThreads)
         stab[t] = __ldg(ker + min(max(t / kTabRep - tabPad, 0), kerSize - 1));
     const float *sker = stab + tabPad * kTabRep + lane % kTabRep; // entry k at sker[k * kTabRep]
     const unsigned tab = (unsigned)__cvta_generic_to_shared(stab) + 4u * (unsigned)(lane % kTabRep) +
                          4u * kTabRep * ((unsigned)tabPad - 0x4B400000u);
-    float *wfoot = sfoot + warp * (kFootH * kFootS);
+    float *wfoot = sfoot + warp * (FH * FS);
     unsigned char *wvox = svox + warp * kWarpVox;
     float *wacc = sacc + warp * kWarpVox;
     float *waccw = saccw + (DENS ? warp * kWarpVox : 0);
@@ -643,13 +524,14 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     // this lane's voxels: x = lx, y = ly, z = bz + s
     const int lx = bx + (lane & 7), ly = by + (lane >> 3);
     const long long R2 = (long long)maskR * maskR;
+    const long long reach2 = ADJ ? (long long)(maskR + 4) * (maskR + 4) : R2;
     unsigned inmask = 0;
 #pragma unroll
     for (int s = 0; s < 4; s++) {
         const int lz = bz + s;
         const long long d2 = (long long)(lx - volCenter) * (lx - volCenter) + (long long)(ly - volCenter) * (ly - volCenter) +
                              (long long)(lz - volCenter) * (lz - volCenter);
-        if (lx < V && ly < V && lz < V && d2 <= R2) inmask |= 1u << s;
+        if (lx < V && ly < V && lz < V && d2 <= reach2) inmask |= 1u << s;
         wacc[lane + 32 * s] = 0.0f;
         if (DENS) waccw[lane + 32 * s] = 0.0f;
     }
@@ -658,7 +540,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     const float kerCenterHalf = kerCenter + 0.5f;
     const float ax0 = (float)lx - volCenter, ay0 = (float)ly - volCenter;
     const float wcx = bx + 3.5f - volCenter, wcy = by + 1.5f - volCenter, wcz = bz + 1.5f - volCenter;
-    const float slab = kerHW + kCullEps;
+    // slab half-thickness: kerHW for the reference rule; for the adjoint, any
+    // voxel within the 4^3 window of a sample point (|r| < 2 per axis)
+    const float slab = ADJ ? 2.0f * 1.7320508f + kCullEps : kerHW + kCullEps;
     const int MM = M * M;
     // Directions are staged through shared memory in chunks, culled against
     // the brick (compacted in order), then against each warp's 8x4x4 block.
@@ -715,14 +599,15 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 const float ext = 0.5f * (7.0f * fabsf(nz0) + 3.0f * fabsf(nz1) + 3.0f * fabsf(nz2));
                 if (fabsf(d) > slab + ext) continue;
             }
-            // the reference's per-voxel slab test (gpuBackProject.cu:64-66);
-            // the active voxels are listed slot by slot, in lane order
+            // the reference's per-voxel slab test (gpuBackProject.cu:64-66), or
+            // the adjoint's reach; the active voxels are listed slot by slot,
+            // in lane order
             int total = 0;
 #pragma unroll
             for (int s = 0; s < 4; s++) {
                 const float az = (float)(bz + s) - volCenter;
                 const float fk = voxel_proj(ax0, ay0, az, nz0, nz1, nz2);
-                const bool act = ((inmask >> s) & 1u) && fabsf(fk) <= kerHW;
+                const bool act = ((inmask >> s) & 1u) && (ADJ ? fabsf(fk) < slab : fabsf(fk) <= kerHW);
                 const unsigned bal = __ballot_sync(0xffffffffu, act);
                 if (act) wvox[total + __popc(bal & lt_mask)] = (unsigned char)(lane + 32 * s);
                 total += __popc(bal);
@@ -740,18 +625,29 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 const float jc = wcx * ny0 + wcy * ny1 + wcz * ny2 + (float)imgCenter;
                 const float hi = 3.5f * fabsf(nx0) + 1.5f * fabsf(nx1) + 1.5f * fabsf(nx2);
                 const float hj = 3.5f * fabsf(ny0) + 1.5f * fabsf(ny1) + 1.5f * fabsf(ny2);
-                fi0 = (int)floorf(ic - hi - 0.6f) - 2;
-                fj0 = (int)floorf(jc - hj - 0.6f) - 2;
-                const int fw = (int)floorf(ic + hi + 0.6f) + 2 - fi0 + 1;
-                fh = (int)floorf(jc + hj + 0.6f) + 2 - fj0 + 1;
-                foot = fw <= kFootW && fh <= kFootH && fh >= 5;
-                if (foot) {
+                fi0 = (int)floorf(ic - hi - 0.6f) - HALF;
+                fj0 = (int)floorf(jc - hj - 0.6f) - HALF;
+                const int fw = (int)floorf(ic + hi + 0.6f) + HALF - fi0 + 1;
+                fh = (int)floorf(jc + hj + 0.6f) + HALF - fj0 + 1;
+                foot = fw <= FW && fh <= FH && fh >= W && (!ADJ || zeroEdges);
+                if (foot && !ADJ) {
+                    // the reference's linear-index rule (gpuBackProject.cu:99)
                     const int c = lane & (kFootW - 1);
                     for (int r = lane >> 4; r < fh; r += 2) {
                         const int lin = (fj0 + r) * M + (fi0 + c);
                         float v = 0.0f;
                         if (lin >= 0 && lin < MM) v = ONES ? 1.0f : ld_f32(img_ptr + lin);
-                        wfoot[r * kFootS + c] = v;
+                        wfoot[r * FS + c] = v;
+                    }
+                } else if (foot) {
+                    // the forward projection's pixels: inside the image and the mask
+                    for (int t = lane; t < fh * FW; t += 32) {
+                        const int r = t / FW, c = t - r * FW;
+                        const int pi = fi0 + c, pj = fj0 + r, di = pi - imgCenter, dj = pj - imgCenter;
+                        float v = 0.0f;
+                        if (pi >= 0 && pi < M && pj >= 0 && pj < M && (long long)di * di + (long long)dj * dj <= R2)
+                            v = ld_f32(img_ptr + (size_t)pj * M + pi);
+                        wfoot[r * FS + c] = v;
                     }
                 }
             }
@@ -769,14 +665,19 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                     const int imgi = (int)roundf(f_imgi);
                     const int imgj = (int)roundf(f_imgj);
                     const bool inside = imgi >= 2 && imgj >= 2 && imgi + 2 < M && imgj + 2 < M;
-                    const int ri = imgi - 2 - fi0, rj = imgj - 2 - fj0;
-                    if (foot && (unsigned)ri <= (unsigned)(kFootW - 5) && (unsigned)rj <= (unsigned)(fh - 5) &&
-                        vi >= 4 && vj >= 4 && vk >= 4 && (inside || !DENS)) {
-                        const FootWin fwin{nx0, nx1, nx2, ny0, ny1, ny2, (float)volCenter, kerScale,
-                                           kerCenterHalf - (float)vi * kerScale, kerCenterHalf - (float)vj * kerScale,
-                                           kerCenterHalf - (float)vk * kerScale};
-                        foot_window<DENS>(fwin, wfoot + rj * kFootS + ri, tab, (float)(imgi - 2 - imgCenter),
-                                          (float)(imgj - 2 - imgCenter), cs, cw);
+                    const int ri = imgi - HALF - fi0, rj = imgj - HALF - fj0;
+                    if (foot && (unsigned)ri <= (unsigned)(FW - W) && (unsigned)rj <= (unsigned)(fh - W) &&
+                        vi >= 4 && vj >= 4 && vk >= 4 && (ADJ || inside || !DENS)) {
+                        // reference rule: index of r = Q - v; adjoint: of r = v - Q
+                        const float sg = ADJ ? -kerScale : kerScale;
+                        const FootWin fwin{nx0, nx1, nx2, ny0, ny1, ny2, (float)volCenter, sg,
+                                           kerCenterHalf - (float)vi * sg, kerCenterHalf - (float)vj * sg,
+                                           kerCenterHalf - (float)vk * sg};
+                        foot_window<DENS, W, FS>(fwin, wfoot + rj * FS + ri, tab, (float)(imgi - HALF - imgCenter),
+                                                 (float)(imgj - HALF - imgCenter), cs, cw);
+                    } else if (ADJ) {
+                        cs = adjoint_window_slow<TI>(vi, vj, vk, volCenter, nx0, nx1, nx2, ny0, ny1, ny2, img_ptr, M,
+                                                     imgCenter, maskR, sker, kerScale, kerCenterHalf, kerSize);
                     } else {
                         const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk,
                                            (float)volCenter, kerScale, kerCenterHalf};
@@ -804,33 +705,21 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     }
 }
 
-template <typename TI, bool ONES, bool DENS = false>
+template <typename TI, bool ONES, bool DENS = false, bool ADJ = false>
 static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
-                                       const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr)
+                                       const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr,
+                                       bool zero_edges = true)
 {
     if (n <= 0) return cudaSuccess;
     const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
     const long long nb = (long long)bx * by * bz;
-    const int pad = bp_table_pad(g.ker_size);
+    const int pad = bp_table_pad(g.ker_size, ADJ);
     const size_t dyn = (size_t)(g.ker_size + 2 * pad) * kTabRep * sizeof(float);
-    auto kern = bp_ref_compact_kernel<TI, ONES, DENS>;
+    auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
     kern<<<(unsigned)nb, kCThreads, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
-                                              g.ker_hw, bx, by, pad, scale);
-    count_launches(1);
-    return cudaGetLastError();
-}
-
-template <typename TI, bool ONES, bool ADJ, bool DENS = false>
-static cudaError_t launch_bp_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
-                               const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr)
-{
-    if (n <= 0) return cudaSuccess;
-    const int bx = (g.V + kBpBX - 1) / kBpBX, by = (g.V + kBpBY - 1) / kBpBY, bz = (g.V + kBpBZ - 1) / kBpBZ;
-    const long long nb = (long long)bx * by * bz;
-    bp_kernel<TI, ONES, ADJ, DENS><<<(unsigned)nb, kBpThreads, 0, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius,
-                                                                       ker, g.ker_size, g.ker_hw, bx, by, scale);
+                                              g.ker_hw, bx, by, pad, zero_edges ? 1 : 0, scale);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -856,11 +745,17 @@ cudaError_t launch_back_project_ref_density(float *d_vol, float *d_pd, const voi
 }
 
 cudaError_t launch_back_project_adjoint(float *d_vol, const void *d_img, int iprec, const float *d_ker,
-                                        const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
+                                        const float *d_axes, int n, const Geom &g, const float *scale, bool zero_edges,
+                                        cudaStream_t s)
 {
-    if (iprec == kF32) return launch_bp_t<float, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
-    if (iprec == kF16) return launch_bp_t<__half, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
-    return launch_bp_t<__nv_bfloat16, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF32)
+        return launch_bp_compact_t<float, false, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s,
+                                                               nullptr, zero_edges);
+    if (iprec == kF16)
+        return launch_bp_compact_t<__half, false, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale,
+                                                                s, nullptr, zero_edges);
+    return launch_bp_compact_t<__nv_bfloat16, false, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n,
+                                                                   g, scale, s, nullptr, zero_edges);
 }
 
 } // namespace gg
