@@ -246,11 +246,9 @@ def run_gb300(args):
         prof[name] = (tot.value, cnt.value)
     check(L.gg_profile_enable(h, 0), h)
     clk = clocks.stop()
-    ms = sum(ms_steps)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    from multigpugridder_gb300.sharding import max_over_ranks
+
+    ms = max_over_ranks(sum(ms_steps), device=dev)  # the slowest rank's time
     ms_per_step = ms / args.steps
     value = world * n / (ms_per_step / 1e3)
 
