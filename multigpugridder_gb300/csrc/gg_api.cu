@@ -150,7 +150,8 @@ struct gg_gridder {
     DevBuf<float> cas;       // FP32 CAS volume V^3 (resident)
     DevBuf<float> cas_fp;    // FP16/BF16 copy the forward projection reads: row pitch
                              // fp_pitch(V) (FP16 scaled by scales[0])
-    bool cas_fp_valid = false;
+    DevBuf<float> cas_y, cas_z; // FP32: the CAS volume with y / z as the contiguous axis
+    bool cas_fp_valid = false;  // cas_fp (FP16/BF16) or cas_y/cas_z (FP32) match cas
     DevBuf<float> pd;        // plane density V^3
     DevBuf<float> adj;       // CAS-volume gradient V^3 (forward-operator adjoint)
     DevBuf<float> axes;
@@ -297,17 +298,34 @@ void check_axes_count(int n)
     if (n < 0) fail(GG_ERR_INVALID_ARG, "n_axes must be >= 0 (got %d)", n);
 }
 
-// Refresh the copy of the CAS volume read by the forward projection (pitched
-// rows, storage precision).
+// Floats taken by one pitched 2-byte copy of the CAS volume (a multiple of 4,
+// so each copy starts 16-byte aligned).
+size_t fp_copy_floats(const gg_gridder *h)
+{
+    return ((size_t)fp_pitch(h->V) * h->V * h->V * prec_bytes(h->prec) + 15) / 16 * 4;
+}
+
+// Refresh the copies of the CAS volume read by the forward projection.
 void update_fp(gg_gridder *h, cudaStream_t s)
 {
-    // FP32 taps are read one by one from the dense volume itself
-    if (h->prec == kF32 || h->cas_fp_valid) return;
+    if (h->cas_fp_valid) return;
+    if (h->prec == kF32) {
+        // FP32 taps are read one by one: the dense volume and its two transposes
+        const size_t V3 = (size_t)h->V * h->V * h->V;
+        h->cas_y.ensure(V3);
+        h->cas_z.ensure(V3);
+        GG_CK(launch_transpose_volume(h->cas.p, h->V, h->cas_y.p, 1, s));
+        GG_CK(launch_transpose_volume(h->cas.p, h->V, h->cas_z.p, 2, s));
+        h->cas_fp_valid = true;
+        return;
+    }
+    // FP16/BF16: three pitched copies with x, y and z contiguous, back to back
     const size_t V3 = (size_t)h->V * h->V * h->V;
-    const int P = fp_pitch(h->V);
-    h->cas_fp.ensure(((size_t)P * h->V * h->V * prec_bytes(h->prec) + 3) / 4);
+    h->cas_fp.ensure(3 * fp_copy_floats(h));
     if (h->prec == kF16) GG_CK(launch_storage_scale(h->cas.p, V3, 8192.0f, h->work.p, h->scales.p, s));
-    GG_CK(launch_pitch_volume(h->cas.p, h->V, P, h->cas_fp.p, h->prec, h->vol_scale(), s));
+    for (int l = 0; l < 3; l++)
+        GG_CK(launch_pitch_volume(h->cas.p, h->V, fp_pitch(h->V), h->cas_fp.p + l * fp_copy_floats(h), h->prec,
+                                  h->vol_scale(), s, l));
     h->cas_fp_valid = true;
 }
 
@@ -348,7 +366,9 @@ void fp_batch(gg_gridder *h, const float *d_axes, int b, float *cas_out, float *
     ProfScope ps(h, s, GG_KERNEL_FORWARD);
     const bool dense = h->prec == kF32;
     GG_CK(launch_forward_project(dense ? h->cas.p : h->cas_fp.p, h->prec, dense ? h->V : fp_pitch(h->V), cas_out,
-                                 h->ker.p, d_axes, b, h->geom(), h->five_taps, h->vol_scale(), s));
+                                 h->ker.p, d_axes, b, h->geom(), h->five_taps, h->vol_scale(), s,
+                                 dense ? (const void *)h->cas_y.p : (const void *)(h->cas_fp.p + fp_copy_floats(h)),
+                                 dense ? (const void *)h->cas_z.p : (const void *)(h->cas_fp.p + 2 * fp_copy_floats(h))));
     ps.done();
     if (img_out) {
         GG_CK(launch_cas_images_to_spectrum(cas_out, h->M, b, S.spec.p, s));
@@ -603,6 +623,8 @@ void destroy_handle(gg_gridder *h)
     h->precomp.release();
     h->cas.release();
     h->cas_fp.release();
+    h->cas_y.release();
+    h->cas_z.release();
     h->pd.release();
     h->adj.release();
     h->axes.release();

@@ -291,14 +291,32 @@ __global__ void convert_kernel(const float *__restrict__ in, T *__restrict__ out
 
 template <typename T>
 __global__ void pitch_volume_kernel(const float *__restrict__ cas, int V, int P, T *__restrict__ out,
-                                    const float *__restrict__ d_scale)
+                                    const float *__restrict__ d_scale, int layout)
 {
     const float inv_scale = d_scale ? 1.0f / *d_scale : 1.0f;
-    const size_t total = (size_t)V * V * P;
+    const size_t total = (size_t)V * V * P, VV = (size_t)V * V;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const size_t row = e / P;
-        const int i = (int)(e - row * P);
-        out[e] = from_f32<T>(i < V ? cas[row * V + i] * inv_scale : 0.0f);
+        const size_t c = e - row * P, b = row % V, a = row / V; // out[a][b][c]
+        float v = 0.0f;
+        if (c < (size_t)V) {
+            // layout 0: [z][y][x]; 1: [z][x][y]; 2: [y][x][z]
+            const size_t x = layout == 0 ? c : b, y = layout == 0 ? b : layout == 1 ? c : a,
+                         z = layout == 2 ? c : a;
+            v = cas[z * VV + y * V + x] * inv_scale;
+        }
+        out[e] = from_f32<T>(v);
+    }
+}
+
+__global__ void transpose_volume_kernel(const float *__restrict__ in, int V, float *__restrict__ out, int layout)
+{
+    const size_t VV = (size_t)V * V, total = VV * V;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t c = e % V, b = (e / V) % V, a = e / VV; // out[a][b][c]
+        // layout 1: [z][x][y] -> (x, y, z) = (b, c, a); layout 2: [y][x][z] -> (b, a, c)
+        const size_t x = b, y = layout == 1 ? c : a, z = layout == 1 ? a : c;
+        out[e] = in[z * VV + y * V + x];
     }
 }
 
@@ -448,12 +466,19 @@ cudaError_t launch_convert(const float *d_in, void *d_out, int prec, size_t coun
 }
 
 cudaError_t launch_pitch_volume(const float *d_cas, int V, int P, void *d_out, int prec, const float *d_scale,
-                                cudaStream_t s)
+                                cudaStream_t s, int layout)
 {
     const unsigned g = grid_for((size_t)V * V * P, kT);
-    if (prec == kF32) pitch_volume_kernel<float><<<g, kT, 0, s>>>(d_cas, V, P, (float *)d_out, d_scale);
-    else if (prec == kF16) pitch_volume_kernel<__half><<<g, kT, 0, s>>>(d_cas, V, P, (__half *)d_out, d_scale);
-    else pitch_volume_kernel<__nv_bfloat16><<<g, kT, 0, s>>>(d_cas, V, P, (__nv_bfloat16 *)d_out, d_scale);
+    if (prec == kF32) pitch_volume_kernel<float><<<g, kT, 0, s>>>(d_cas, V, P, (float *)d_out, d_scale, layout);
+    else if (prec == kF16) pitch_volume_kernel<__half><<<g, kT, 0, s>>>(d_cas, V, P, (__half *)d_out, d_scale, layout);
+    else pitch_volume_kernel<__nv_bfloat16><<<g, kT, 0, s>>>(d_cas, V, P, (__nv_bfloat16 *)d_out, d_scale, layout);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_transpose_volume(const float *d_in, int V, float *d_out, int layout, cudaStream_t s)
+{
+    transpose_volume_kernel<<<grid_for((size_t)V * V * V, kT), kT, 0, s>>>(d_in, V, d_out, layout);
     count_launches(1);
     return cudaGetLastError();
 }

@@ -33,14 +33,24 @@ struct Geom {
 // The volume's rows are `pitch` elements apart (planes pitch*V); the
 // reference's dense layout is pitch = V.  fp_pitch(V) rows let the 4-tap
 // kernel read each row of taps with aligned vector loads.
+// d_vol_y, d_vol_z (optional): copies of the volume, in the same storage and
+// pitch, with y and z as the contiguous axis (launch_transpose_volume for
+// dense FP32, launch_pitch_volume layouts 1 and 2 for FP16/BF16); each
+// direction then reads the copy whose contiguous axis is the most
+// perpendicular to it.
 cudaError_t launch_forward_project(const void *d_vol, int vprec, int pitch, float *d_img, const float *d_ker,
                                    const float *d_axes, int n, const Geom &g, bool five_taps,
-                                   const float *d_scale, cudaStream_t s);
+                                   const float *d_scale, cudaStream_t s, const void *d_vol_y = nullptr,
+                                   const void *d_vol_z = nullptr);
+// FP32 volume V^3 (x fastest) -> the same volume with y (layout 1: [z][x][y])
+// or z (layout 2: [y][x][z]) as the contiguous axis.
+cudaError_t launch_transpose_volume(const float *d_in, int V, float *d_out, int layout, cudaStream_t s);
 inline int fp_pitch(int V) { return (V + 4 + 7) / 8 * 8; }
 // FP32 CAS volume V^3 -> the same volume with row pitch P (zero-filled past
-// V) in storage `prec` (x / *d_scale for FP16).
+// V) in storage `prec` (x / *d_scale for FP16), with x (layout 0: [z][y][x]),
+// y (layout 1: [z][x][y]) or z (layout 2: [y][x][z]) as the contiguous axis.
 cudaError_t launch_pitch_volume(const float *d_cas, int V, int P, void *d_out, int prec, const float *d_scale,
-                                cudaStream_t s);
+                                cudaStream_t s, int layout = 0);
 
 // Back projection with the reference window rule, accumulated (+=) into the
 // FP32 CAS volume.  d_img holds n*M*M CAS images in storage `iprec`; when

@@ -123,11 +123,20 @@ __device__ __forceinline__ void ld8(const __nv_bfloat16 *p, float v[8])
     }
 }
 
-template <typename TV, int TAPS, bool VEC>
+// TR: two more copies of the volume with y and z as the contiguous axis
+// (volY[z][x][y], volZ[y][x][z]).  A warp's 8x4 pixels touch about
+// 32 |n . e_c| + (perimeter) distinct volume rows per gather, e_c the
+// contiguous axis and n the viewing direction, so each direction reads the
+// copy whose contiguous axis is the most perpendicular to n.  FP32 (dense
+// copies): each thread still sums its taps in the same order, so the results
+// are identical.  VEC (pitched 2-byte copies): the rows of taps are read along
+// the copy's contiguous axis, which changes only the order of the sums.
+template <typename TV, int TAPS, bool VEC, bool TR = false>
 __global__ void __launch_bounds__(kFpThreads)
 fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int M,
           const float *__restrict__ axes, int maskR, const float *__restrict__ ker, int kerSize,
-          float kerHW, int tilesX, long long nItems, const float *__restrict__ d_scale)
+          float kerHW, int tilesX, long long nItems, const float *__restrict__ d_scale,
+          const TV *__restrict__ volY, const TV *__restrict__ volZ)
 {
     const float outScale = d_scale ? *d_scale : 1.0f;
     __shared__ float sker[kMaxKerSize];
@@ -194,12 +203,28 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
         float acc = 0.0f;
         const bool inside = b0 >= 0 && b1 >= 0 && b2 >= 0 && b0 + TAPS <= V && b1 + TAPS <= V && b2 + TAPS <= V;
         if (VEC && inside) {
-            const int sft = b0 & 3;
+            // the copy (layout 0: x, 1: y, 2: z contiguous) and its axes, fastest first
+            int lay = 0;
+            if (TR) {
+                const float nz0 = fabsf(__ldg(ax + 6)), nz1 = fabsf(__ldg(ax + 7)), nz2 = fabsf(__ldg(ax + 8));
+                lay = (nz1 < nz0 && nz1 <= nz2) ? 1 : (nz2 < nz0 && nz2 < nz1) ? 2 : 0;
+            }
+            const int bc = lay == 0 ? b0 : lay == 1 ? b1 : b2;       // contiguous axis
+            const int bb = lay == 0 ? b1 : b0;                        // middle axis
+            const int ba = lay == 2 ? b1 : b2;                        // outer axis
+            float wc[TAPS], wb[TAPS], wa[TAPS];
+#pragma unroll
+            for (int d = 0; d < TAPS; d++) {
+                wc[d] = lay == 0 ? wi[d] : lay == 1 ? wj[d] : wk[d];
+                wb[d] = lay == 0 ? wj[d] : wi[d];
+                wa[d] = lay == 2 ? wj[d] : wk[d];
+            }
+            const int sft = bc & 3;
             float w8[8];
 #pragma unroll
             for (int t = 0; t < 8; t++)
-                w8[t] = t == sft ? wi[0] : t == sft + 1 ? wi[1] : t == sft + 2 ? wi[2] : t == sft + 3 ? wi[3] : 0.0f;
-            const TV *base = vol + (size_t)b2 * PV + (size_t)b1 * P + (b0 - sft);
+                w8[t] = t == sft ? wc[0] : t == sft + 1 ? wc[1] : t == sft + 2 ? wc[2] : t == sft + 3 ? wc[3] : 0.0f;
+            const TV *base = (lay == 0 ? vol : lay == 1 ? volY : volZ) + (size_t)ba * PV + (size_t)bb * P + (bc - sft);
 #pragma unroll
             for (int dk = 0; dk < TAPS; dk++) {
 #pragma unroll
@@ -209,6 +234,25 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
                     float s = 0.0f;
 #pragma unroll
                     for (int t = 0; t < 8; t++) s = fmaf(w8[t], v[t], s);
+                    acc = fmaf(wb[dj2] * wa[dk], s, acc);
+                }
+            }
+        } else if (TR && inside) {
+            const float nz0 = fabsf(__ldg(ax + 6)), nz1 = fabsf(__ldg(ax + 7)), nz2 = fabsf(__ldg(ax + 8));
+            const int lay = (nz1 < nz0 && nz1 <= nz2) ? 1 : (nz2 < nz0 && nz2 < nz1) ? 2 : 0;
+            // element strides of x, y, z in the chosen copy
+            const size_t sx = lay == 0 ? 1 : (size_t)V;
+            const size_t sy = lay == 0 ? (size_t)V : lay == 1 ? 1 : VV;
+            const size_t sz = lay == 2 ? 1 : VV;
+            const TV *base = (lay == 0 ? vol : lay == 1 ? volY : volZ) + b0 * sx + b1 * sy + b2 * sz;
+#pragma unroll
+            for (int dk = 0; dk < TAPS; dk++) {
+#pragma unroll
+                for (int dj2 = 0; dj2 < TAPS; dj2++) {
+                    const TV *p = base + dk * sz + dj2 * sy;
+                    float s = 0.0f;
+#pragma unroll
+                    for (int d = 0; d < TAPS; d++) s = fmaf(wi[d], ld_f32(p + d * sx), s);
                     acc = fmaf(wj[dj2] * wk[dk], s, acc);
                 }
             }
@@ -242,44 +286,54 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
     }
 }
 
-template <typename TV, int TAPS, bool VEC>
+template <typename TV, int TAPS, bool VEC, bool TR = false>
 static cudaError_t launch_fp_t(const TV *vol, int P, float *img, const float *ker, const float *axes, int n,
-                               const Geom &g, const float *scale, cudaStream_t s)
+                               const Geom &g, const float *scale, cudaStream_t s, const TV *volY = nullptr,
+                               const TV *volZ = nullptr)
 {
     const int tilesX = (g.M + kFpTile - 1) / kFpTile;
     const long long nItems = (long long)n * tilesX * tilesX;
     if (nItems == 0) return cudaSuccess;
     int perSm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fp_kernel<TV, TAPS, VEC>, kFpThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fp_kernel<TV, TAPS, VEC, TR>, kFpThreads, 0);
     if (perSm <= 0) perSm = 1;
     long long grid = (long long)num_sms() * perSm;
     if (grid > nItems) grid = nItems;
-    fp_kernel<TV, TAPS, VEC><<<(unsigned)grid, kFpThreads, 0, s>>>(vol, g.V, P, img, g.M, axes, g.mask_radius, ker,
-                                                                    g.ker_size, g.ker_hw, tilesX, nItems, scale);
+    fp_kernel<TV, TAPS, VEC, TR><<<(unsigned)grid, kFpThreads, 0, s>>>(vol, g.V, P, img, g.M, axes, g.mask_radius,
+                                                                        ker, g.ker_size, g.ker_hw, tilesX, nItems,
+                                                                        scale, volY, volZ);
     count_launches(1);
     return cudaGetLastError();
 }
 
 template <typename TV>
 static cudaError_t launch_fp_p(const void *d_vol, int P, float *d_img, const float *d_ker, const float *d_axes, int n,
-                               const Geom &g, bool five_taps, const float *scale, cudaStream_t s)
+                               const Geom &g, bool five_taps, const float *scale, cudaStream_t s,
+                               const void *d_vol_y, const void *d_vol_z)
 {
     const TV *v = (const TV *)d_vol;
     if (five_taps) return launch_fp_t<TV, 5, false>(v, P, d_img, d_ker, d_axes, n, g, scale, s);
+    const TV *vy = (const TV *)d_vol_y, *vz = (const TV *)d_vol_z;
+    if (sizeof(TV) == 4 && vy && vz && P == g.V)
+        return launch_fp_t<TV, 4, false, true>(v, P, d_img, d_ker, d_axes, n, g, scale, s, vy, vz);
     // 2-byte storage only: with FP32 the 8-element rows double the bytes each
     // tap row moves through L1, which costs more than the loads it saves
     const bool vec = sizeof(TV) == 2 && P % 8 == 0 && P >= g.V + 4 && ((size_t)d_vol & 15) == 0;
+    const bool aligned = ((size_t)vy & 15) == 0 && ((size_t)vz & 15) == 0;
+    if (vec && vy && vz && aligned) return launch_fp_t<TV, 4, true, true>(v, P, d_img, d_ker, d_axes, n, g, scale, s, vy, vz);
     if (vec) return launch_fp_t<TV, 4, true>(v, P, d_img, d_ker, d_axes, n, g, scale, s);
     return launch_fp_t<TV, 4, false>(v, P, d_img, d_ker, d_axes, n, g, scale, s);
 }
 
 cudaError_t launch_forward_project(const void *d_vol, int vprec, int pitch, float *d_img, const float *d_ker,
                                    const float *d_axes, int n, const Geom &g, bool five_taps, const float *scale,
-                                   cudaStream_t s)
+                                   cudaStream_t s, const void *d_vol_y, const void *d_vol_z)
 {
-    if (vprec == kF32) return launch_fp_p<float>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s);
-    if (vprec == kF16) return launch_fp_p<__half>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s);
-    return launch_fp_p<__nv_bfloat16>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s);
+    if (vprec == kF32)
+        return launch_fp_p<float>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s, d_vol_y, d_vol_z);
+    if (vprec == kF16)
+        return launch_fp_p<__half>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s, d_vol_y, d_vol_z);
+    return launch_fp_p<__nv_bfloat16>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s, d_vol_y, d_vol_z);
 }
 
 // ---------------------------------------------------------------------------
