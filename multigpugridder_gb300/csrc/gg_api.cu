@@ -1238,8 +1238,20 @@ bool gg::gridder_view(gg_gridder *h, GridderView *out)
 {
     if (!h || !h->cas.p) return false;
     std::lock_guard<std::mutex> lock(h->mu);
-    *out = GridderView{h->device, h->N, h->M, h->V, h->geom(), h->cas.p, h->ker.p, h->five_taps};
+    const bool t = h->prec == kF32 && h->cas_fp_valid;
+    *out = GridderView{h->device, h->N, h->M, h->V, h->geom(), h->cas.p, t ? h->cas_y.p : nullptr,
+                       t ? h->cas_z.p : nullptr, h->ker.p, h->five_taps};
     return true;
+}
+
+bool gg::gridder_prepare_forward(gg_gridder *h)
+{
+    return guarded(h, [&] {
+        set_device(h);
+        require_volume(h);
+        update_fp(h, h->cs);
+        GG_CK(cudaStreamSynchronize(h->cs));
+    }) == GG_OK;
 }
 
 void gg::gridder_trim(gg_gridder *h)

@@ -135,6 +135,7 @@ struct GridderView {
     int device, N, M, V;
     Geom g;
     const float *cas; // FP32 CAS volume V^3
+    const float *cas_y, *cas_z; // its copies with y / z contiguous (may be null)
     const float *ker; // KB table
     bool five_taps;
 };
@@ -150,6 +151,9 @@ bool gridder_view(gg_gridder *h, GridderView *out);
 // Frees the gridder's set-up scratch (the M^3 FFT buffers and plans); the
 // CAS volume stays resident.
 void gridder_trim(gg_gridder *h);
+// Builds the copies of the CAS volume the FP32 forward projection reads
+// (synchronous); false on failure.
+bool gridder_prepare_forward(gg_gridder *h);
 
 // ---- host math (gg_kb.cpp) --------------------------------------------------
 void kb_table_f64(int hw, int size, double *out);

@@ -249,7 +249,7 @@ void enqueue(gg_server *S, Request &r)
         const cufftHandle p = lane_plan(L, r.op == GG_OP_FORWARD ? CUFFT_C2R : CUFFT_R2C, v.M, pow2ceil(b));
         if (r.op == GG_OP_FORWARD) {
             GS_CK(launch_forward_project(v.cas, kF32, v.V, d_cas, v.ker, d_axes + (size_t)c0 * 9, b, v.g, v.five_taps,
-                                         nullptr, s));
+                                         nullptr, s, v.cas_y, v.cas_z));
             GS_CK(launch_cas_images_to_spectrum(d_cas, v.M, b, d_spec, s));
             GS_CKF(cufftExecC2R(p, d_spec, d_real));
             GS_CK(launch_fft_output_to_images(d_real, v.M, v.N, b, d_img, s));
@@ -472,6 +472,11 @@ extern "C" int gg_server_add_volume(gg_server *S, const float *volume, int volum
             sfail(rc, "setting the volume: %s", m.c_str());
         }
         gridder_trim(h);
+        if (!gridder_prepare_forward(h)) {
+            std::string m = gg_last_error(h);
+            gg_destroy(h);
+            sfail(GG_ERR_CUDA, "preparing the volume copies: %s", m.c_str());
+        }
         Volume v;
         if (!gridder_view(h, &v.view)) {
             gg_destroy(h);
