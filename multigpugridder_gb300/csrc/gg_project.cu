@@ -447,19 +447,19 @@ struct FootWin {
     float c0, c1, c2; // h - v*s per axis
 };
 
-// One voxel's W x W window from the footprint (fbase = its top-left pixel,
+// One voxel's WI x WJ window from the footprint (fbase = its top-left pixel,
 // rows FS apart); table entry floor(x) is read at
 // tab + bits(x + 1.5*2^23) * 4 * kTabRep.  Sums row by row, as the reference.
-template <bool DENS, int W, int FS>
+template <bool DENS, int WI, int WJ, int FS>
 __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase, unsigned tab, float pi0, float pj0,
                                             float &cumSum, float &cumW)
 {
 #pragma unroll
-    for (int jo = 0; jo < W; jo++) {
+    for (int jo = 0; jo < WJ; jo++) {
         const float pj = pj0 + (float)jo;
         const float py0 = __fmul_rn(pj, q.ny0), py1 = __fmul_rn(pj, q.ny1), py2 = __fmul_rn(pj, q.ny2);
 #pragma unroll
-        for (int io = 0; io < W; io++) {
+        for (int io = 0; io < WI; io++) {
             const float pi = pi0 + (float)io;
             const float q0 = __fadd_rn(__fmaf_rn(pi, q.nx0, py0), q.vc);
             const float q1 = __fadd_rn(__fmaf_rn(pi, q.nx1, py1), q.vc);
@@ -648,6 +648,13 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             const int al = e & (kBpChunk - 1);
             const float *ax = sax + al * 9;
             const float nz0 = ax[6], nz1 = ax[7], nz2 = ax[8];
+            // Adjoint, orthonormal axes: a pixel weighs non-zero only if its
+            // sample point f lies in the voxel's cube |f - v| < 2 (each axis),
+            // which the plane reaches only if |f_k| < 2 |nz|_1: a slab
+            // thinner than 2 sqrt(3) for most directions.
+            const float slabD = ADJ && (e & kBpChunk)
+                                    ? fminf(slab, 2.0f * (fabsf(nz0) + fabsf(nz1) + fabsf(nz2)) + kCullEps)
+                                    : slab;
             {   // the warp's 8x4x4 block against the slab (uniform)
                 const float d = wcx * nz0 + wcy * nz1 + wcz * nz2;
                 const float ext = 0.5f * (7.0f * fabsf(nz0) + 3.0f * fabsf(nz1) + 3.0f * fabsf(nz2));
@@ -661,7 +668,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             for (int s = 0; s < 4; s++) {
                 const float az = (float)(bz + s) - volCenter;
                 const float fk = voxel_proj(ax0, ay0, az, nz0, nz1, nz2);
-                const bool act = ((inmask >> s) & 1u) && (ADJ ? fabsf(fk) < slab : fabsf(fk) <= kerHW);
+                const bool act = ((inmask >> s) & 1u) && (ADJ ? fabsf(fk) < slabD : fabsf(fk) <= kerHW);
                 const unsigned bal = __ballot_sync(0xffffffffu, act);
                 if (act) wvox[total + __popc(bal & lt_mask)] = (unsigned char)(lane + 32 * s);
                 total += __popc(bal);
@@ -727,8 +734,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                         const FootWin fwin{nx0, nx1, nx2, ny0, ny1, ny2, (float)volCenter, sg,
                                            kerCenterHalf - (float)vi * sg, kerCenterHalf - (float)vj * sg,
                                            kerCenterHalf - (float)vk * sg};
-                        foot_window<DENS, W, FS>(fwin, wfoot + rj * FS + ri, tab, (float)(imgi - HALF - imgCenter),
-                                                 (float)(imgj - HALF - imgCenter), cs, cw);
+                        const float *fb = wfoot + rj * FS + ri;
+                        const float pi0 = (float)(imgi - HALF - imgCenter), pj0 = (float)(imgj - HALF - imgCenter);
+                        foot_window<DENS, W, W, FS>(fwin, fb, tab, pi0, pj0, cs, cw);
                     } else if (ADJ) {
                         cs = adjoint_window_slow<TI>(vi, vj, vk, volCenter, nx0, nx1, nx2, ny0, ny1, ny2, img_ptr, M,
                                                      imgCenter, maskR, sker, kerScale, kerCenterHalf, kerSize);
