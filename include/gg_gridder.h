@@ -138,6 +138,26 @@ int gg_get_volume_dev(gg_gridder *h, float *d_volume_out, void *stream);
 int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int n_axes,
                               const float *d_images, float *d_volume_out, void *stream);
 
+/* reconstructVol with CTF correction.  The reference carries only the flag
+   for it (`ApplyCTFs`, src/Gridders/AbstractGridder.h:118-119) and never
+   reads it.  Each image's CAS image is multiplied by its weak-phase CTF
+   before the back projection, and the plane density back-projects CTF^2
+   images instead of all-ones ones:
+     vol = getVol( BP(CTF . CAS(img)) ./ (BP(CTF^2) + 1e-6) ).
+   CTF(s) = -(sqrt(1 - A^2) sin chi + A cos chi),
+   chi = pi lambda df s^2 - (pi/2) Cs lambda^3 s^4, s the spatial frequency
+   (1/Å) of the padded image's pixel, lambda the relativistic electron
+   wavelength at voltage_kv.  defocus: n_axes values in Å (underfocus
+   positive); cs_mm in mm; amp_contrast A in [0, 1]; pixel_size: Å per pixel
+   of the N x N images.  With defocus 0, Cs 0 and A = 1 the CTF is -1 and the
+   result equals gg_reconstruct_volume's. */
+int gg_reconstruct_volume_ctf(gg_gridder *h, const float *axes, int n_axes, const float *images,
+                              const float *defocus, float voltage_kv, float cs_mm, float amp_contrast,
+                              float pixel_size, float *volume_out);
+int gg_reconstruct_volume_ctf_dev(gg_gridder *h, const float *d_axes, int n_axes, const float *d_images,
+                                  const float *d_defocus, float voltage_kv, float cs_mm, float amp_contrast,
+                                  float pixel_size, float *d_volume_out, void *stream);
+
 /* Exact adjoint of the whole forward operator (setVolume's CAS preparation
    followed by forwardProject to images): image gradients n*N*N -> volume
    gradient N^3 (written, not accumulated).  Uses the exact-adjoint back
@@ -210,6 +230,13 @@ int gg_filter_add_volumes(float *d_a, const float *d_b, int size, int n_slices, 
 int gg_filter_divide_scalar(float *d_a, float scalar, int size, int n_slices, void *stream);                  /* DivideScalarFilter.cu:3-25 */
 int gg_filter_real_to_complex(const float *d_real, float *d_complex, int size, int n_slices, void *stream);   /* RealToComplexFilter.cu:3-26 */
 int gg_filter_complex_to_real(const float *d_complex, float *d_real, int size, int n_slices, void *stream);   /* ComplexToRealFilter.cu:3-25 */
+
+/* CTF on CAS images (n_images * size^2, the gridder's CAS-image layout, DC at
+   (size/2, size/2)): generate = 0 multiplies them by CTF^power, generate = 1
+   overwrites them with CTF^power (power 1 or 2).  Parameters as for
+   gg_reconstruct_volume_ctf.  No counterpart in the reference. */
+int gg_filter_apply_ctf(float *d_cas_images, int size, int n_images, const float *d_defocus, float voltage_kv,
+                        float cs_mm, float amp_contrast, float pixel_size, int power, int generate, void *stream);
 
 /* Host helpers: the KB lookup table (getKernelFiltTable.m:1-22) and the
    pre-compensation vector (getPreComp.m:1-28), computed in FP64. */

@@ -436,6 +436,31 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
     }
 }
 
+// One batch of the CTF-corrected reconstruction: the images' CAS images times
+// the CTF are back-projected into h->cas, and CTF^2 images into h->pd (the
+// CTF-weighted plane density), both by the gridder's back-projection rule.
+void ctf_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const float *d_defocus,
+               const CtfParams &c, int sl, cudaStream_t s)
+{
+    auto &S = h->slot[sl];
+    GG_CK(launch_images_to_fft_input(img, h->N, h->M, b, S.real.p, s));
+    cufftHandle p = plan2d(h, CUFFT_R2C, b);
+    GG_CKF(cufftSetStream(p, s));
+    GG_CKF(cufftExecR2C(p, S.real.p, S.spec.p));
+    GG_CK(launch_spectrum_to_cas_images(S.spec.p, h->M, b, S.casimg.p, kF32, nullptr, s));
+    // CAS images *= CTF, and CTF^2 into S.real (free after the R2C), in one pass
+    GG_CK(launch_ctf(S.casimg.p, 1, S.real.p, 2, h->M, b, d_defocus, c, s));
+    bp_batch(h, d_axes, b, nullptr, S.casimg.p, h->cas.p, false, sl, s);
+    bp_batch(h, d_axes, b, nullptr, S.real.p, h->pd.p, false, sl, s);
+}
+
+void check_ctf(const CtfParams &c)
+{
+    if (!(c.voltage_kv > 0.0f) || !(c.pixel_size > 0.0f) || !(c.amp_contrast >= 0.0f && c.amp_contrast <= 1.0f) ||
+        !std::isfinite(c.cs_mm) || !std::isfinite(c.voltage_kv) || !std::isfinite(c.pixel_size))
+        fail(GG_ERR_INVALID_ARG, "CTF needs voltage > 0, pixel size > 0, 0 <= amplitude contrast <= 1, finite Cs");
+}
+
 // Exact adjoint of (CAS preparation + forward projection + CAS images ->
 // images): image gradients (device, n*N*N) -> volume gradient (device, N^3).
 void forward_adjoint(gg_gridder *h, const float *d_axes, int n, const float *d_img_grad, float *d_vol_grad, cudaStream_t s)
@@ -1079,6 +1104,77 @@ extern "C" int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int
         do_get_volume(h, h->cas.p, d_volume_out, s);
         h->cas_fp_valid = false;
         end_dev(h, s);
+    });
+}
+
+extern "C" int gg_reconstruct_volume_ctf_dev(gg_gridder *h, const float *d_axes, int n_axes, const float *d_images,
+                                             const float *d_defocus, float voltage_kv, float cs_mm, float amp_contrast,
+                                             float pixel_size, float *d_volume_out, void *stream)
+{
+    return guarded(h, [&] {
+        check_axes_count(n_axes);
+        if (n_axes > 0 && (!d_axes || !d_images || !d_defocus))
+            fail(GG_ERR_INVALID_ARG, "axes, images and defocus are required");
+        if (!d_volume_out) fail(GG_ERR_INVALID_ARG, "output is NULL");
+        const CtfParams c{voltage_kv, cs_mm, amp_contrast, pixel_size};
+        check_ctf(c);
+        cudaStream_t s = (cudaStream_t)stream;
+        begin_dev(h, s);
+        const size_t V3 = (size_t)h->V * h->V * h->V, NN = (size_t)h->N * h->N;
+        h->cas.ensure(V3);
+        h->pd.ensure(V3);
+        GG_CK(cudaMemsetAsync(h->cas.p, 0, V3 * sizeof(float), s));
+        GG_CK(cudaMemsetAsync(h->pd.p, 0, V3 * sizeof(float), s));
+        const int B = h->max_batch;
+        for (int a0 = 0; a0 < n_axes; a0 += B) {
+            const int b = std::min(B, n_axes - a0);
+            ensure_slot(h, 0, B, false);
+            ctf_batch(h, d_axes + (size_t)a0 * 9, b, d_images + (size_t)a0 * NN, d_defocus + a0, c, 0, s);
+        }
+        GG_CK(launch_divide_plane_density(h->cas.p, h->pd.p, V3, 1e-6f, s));
+        do_get_volume(h, h->cas.p, d_volume_out, s);
+        h->cas_fp_valid = false;
+        end_dev(h, s);
+    });
+}
+
+extern "C" int gg_reconstruct_volume_ctf(gg_gridder *h, const float *axes, int n_axes, const float *images,
+                                         const float *defocus, float voltage_kv, float cs_mm, float amp_contrast,
+                                         float pixel_size, float *volume_out)
+{
+    return guarded(h, [&] {
+        check_axes_count(n_axes);
+        if (n_axes > 0 && (!axes || !images || !defocus))
+            fail(GG_ERR_INVALID_ARG, "axes, images and defocus are required");
+        if (!volume_out) fail(GG_ERR_INVALID_ARG, "output is NULL");
+        const CtfParams c{voltage_kv, cs_mm, amp_contrast, pixel_size};
+        check_ctf(c);
+        cudaStream_t s = h->cs;
+        const size_t V3 = (size_t)h->V * h->V * h->V, NN = (size_t)h->N * h->N, N3 = NN * h->N;
+        upload_axes(h, axes, n_axes, s);
+        DevBuf<float> df;
+        df.ensure((size_t)std::max(1, n_axes));
+        if (n_axes > 0) GG_CK(cudaMemcpyAsync(df.p, defocus, (size_t)n_axes * sizeof(float), cudaMemcpyHostToDevice, s));
+        h->cas.ensure(V3);
+        h->pd.ensure(V3);
+        GG_CK(cudaMemsetAsync(h->cas.p, 0, V3 * sizeof(float), s));
+        GG_CK(cudaMemsetAsync(h->pd.p, 0, V3 * sizeof(float), s));
+        const int B = h->max_batch;
+        for (int a0 = 0; a0 < n_axes; a0 += B) {
+            const int b = std::min(B, n_axes - a0);
+            ensure_slot(h, 0, B, true);
+            auto &S = h->slot[0];
+            GG_CK(cudaMemcpyAsync(S.img.p, images + (size_t)a0 * NN, (size_t)b * NN * sizeof(float),
+                                  cudaMemcpyHostToDevice, s));
+            ctf_batch(h, h->axes.p + (size_t)a0 * 9, b, S.img.p, df.p + a0, c, 0, s);
+        }
+        GG_CK(launch_divide_plane_density(h->cas.p, h->pd.p, V3, 1e-6f, s));
+        h->vol_io.ensure(N3);
+        do_get_volume(h, h->cas.p, h->vol_io.p, s);
+        GG_CK(cudaMemcpyAsync(volume_out, h->vol_io.p, N3 * sizeof(float), cudaMemcpyDeviceToHost, s));
+        GG_CK(cudaStreamSynchronize(s));
+        df.release();
+        h->cas_fp_valid = false;
     });
 }
 

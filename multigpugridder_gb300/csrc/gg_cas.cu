@@ -14,6 +14,8 @@
 //     spectrum is read through conjugate symmetry when forming Re+Im.
 #include <stdint.h>
 
+#include <cmath>
+
 #include "gg_common.cuh"
 #include "gg_internal.h"
 #include "../../include/gg_gridder.h"
@@ -320,6 +322,51 @@ __global__ void transpose_volume_kernel(const float *__restrict__ in, int V, flo
     }
 }
 
+// Weak-phase CTF at each CAS-image pixel, r2 = |(i, j) - M/2|^2 (an exact
+// integer): chi = r2 (alpha df) - r2^2 beta with alpha = pi lambda / (M px)^2,
+// beta = pi/2 Cs lambda^3 / (M px)^4; CTF = -(sqrt(1 - A^2) sin chi + A cos chi).
+// chi reaches hundreds of radians, so it is formed in float-float arithmetic
+// (Dekker's error-free products through fmaf, Knuth's two-sum) and reduced
+// mod 2 pi by Cody and Waite's method with 2 pi split into three parts (the
+// first two short enough that k * part is exact); sincosf then sees |r| <= pi.
+// A real, even CTF multiplies Re and Im alike, so it applies to CAS images
+// directly.  d_mul (optional) *= CTF^mul_power; d_gen (optional) = CTF^gen_power.
+__global__ void ctf_kernel(float *__restrict__ d_mul, float *__restrict__ d_gen, int M, int n,
+                           const float *__restrict__ defocus, CtfConsts k, int mul_power, int gen_power)
+{
+    const size_t MM = (size_t)M * M, total = MM * n;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t a = e / MM, r = e - a * MM;
+        const int di = (int)(r % M) - M / 2, dj = (int)(r / M) - M / 2;
+        const float r2 = (float)(di * di + dj * dj);
+        const float df = defocus[a];
+        // c = alpha * df as hi + lo
+        const float c_hi = k.a_hi * df;
+        const float c_lo = fmaf(k.a_hi, df, -c_hi) + k.a_lo * df;
+        // t1 = r2 * c
+        const float t1_hi = r2 * c_hi;
+        const float t1_lo = fmaf(r2, c_hi, -t1_hi) + r2 * c_lo;
+        // t2 = r2^2 * beta
+        const float q_hi = r2 * r2, q_lo = fmaf(r2, r2, -q_hi);
+        const float t2_hi = q_hi * k.b_hi;
+        const float t2_lo = fmaf(q_hi, k.b_hi, -t2_hi) + q_hi * k.b_lo + q_lo * k.b_hi;
+        // chi = t1 - t2 (two-sum of the high parts)
+        const float d_hi = t1_hi - t2_hi;
+        const float bb = d_hi - t1_hi, aa = d_hi - bb;
+        const float d_lo = ((t1_hi - aa) + (-t2_hi - bb)) + (t1_lo - t2_lo);
+        // reduction mod 2 pi
+        const float kk = rintf(d_hi * k.inv_2pi);
+        float red = fmaf(-kk, k.p1, d_hi);
+        red = fmaf(-kk, k.p2, red);
+        red = fmaf(-kk, k.p3, red) + d_lo;
+        float sn, cs;
+        sincosf(red, &sn, &cs);
+        const float ctf = -(k.w_sin * sn + k.w_cos * cs);
+        if (d_mul) d_mul[e] *= mul_power == 2 ? ctf * ctf : ctf;
+        if (d_gen) d_gen[e] = gen_power == 2 ? ctf * ctf : ctf;
+    }
+}
+
 // Non-negative floats order like their bit patterns, so an unsigned atomicMax
 // on the bits of |x| finds the largest magnitude.
 __global__ void max_abs_kernel(const float *__restrict__ x, size_t count, unsigned int *out)
@@ -479,6 +526,47 @@ cudaError_t launch_pitch_volume(const float *d_cas, int V, int P, void *d_out, i
 cudaError_t launch_transpose_volume(const float *d_in, int V, float *d_out, int layout, cudaStream_t s)
 {
     transpose_volume_kernel<<<grid_for((size_t)V * V * V, kT), kT, 0, s>>>(d_in, V, d_out, layout);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+static void split_f(double x, float *hi, float *lo)
+{
+    *hi = (float)x;
+    *lo = (float)(x - (double)*hi);
+}
+
+// 2 pi to `bits` significant bits (towards zero), so that k * part is exact
+// in FP32 for |k| < 2^(24 - bits).
+static double leading_bits(double x, int bits)
+{
+    int ex;
+    const double m = std::frexp(x, &ex);
+    return std::ldexp(std::trunc(std::ldexp(m, bits)), ex - bits);
+}
+
+cudaError_t launch_ctf(float *d_mul, int mul_power, float *d_gen, int gen_power, int M, int n, const float *d_defocus,
+                       const CtfParams &c, cudaStream_t s)
+{
+    if (n <= 0 || (!d_mul && !d_gen)) return cudaSuccess;
+    // electron wavelength (Å) at the accelerating voltage, relativistic
+    const double U = (double)c.voltage_kv * 1e3;
+    const double lambda = 12.2643247 / std::sqrt(U * (1.0 + 0.978466e-6 * U));
+    const double pi = 3.14159265358979323846;
+    const double q = 1.0 / (((double)M * c.pixel_size) * ((double)M * c.pixel_size));
+    const double alpha = pi * lambda * q, beta = 0.5 * pi * ((double)c.cs_mm * 1e7) * lambda * lambda * lambda * q * q;
+    CtfConsts k;
+    split_f(alpha, &k.a_hi, &k.a_lo);
+    split_f(beta, &k.b_hi, &k.b_lo);
+    const double p1 = leading_bits(2 * pi, 12), p2 = leading_bits(2 * pi - p1, 12);
+    k.p1 = (float)p1;
+    k.p2 = (float)p2;
+    k.p3 = (float)(2 * pi - p1 - p2);
+    k.inv_2pi = (float)(1.0 / (2 * pi));
+    const double A = c.amp_contrast;
+    k.w_sin = (float)std::sqrt(1.0 - A * A);
+    k.w_cos = (float)A;
+    ctf_kernel<<<grid_for((size_t)M * M * n, kT), kT, 0, s>>>(d_mul, d_gen, M, n, d_defocus, k, mul_power, gen_power);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -734,4 +822,19 @@ extern "C" int gg_filter_complex_to_real(const float *d_complex, float *d_real, 
     const size_t c = slice_count(size, n_slices);
     f_complex_to_real<<<grid_for(c, kT), kT, 0, (cudaStream_t)stream>>>((const float2 *)d_complex, d_real, c);
     GG_FILTER_RET();
+}
+
+extern "C" int gg_filter_apply_ctf(float *d_cas_images, int cas_img_size, int n_images, const float *d_defocus,
+                                   float voltage_kv, float cs_mm, float amp_contrast, float pixel_size, int power,
+                                   int generate, void *stream)
+{
+    if (cas_img_size <= 0 || n_images < 0 || (n_images > 0 && (!d_cas_images || !d_defocus)) ||
+        (power != 1 && power != 2) || !(voltage_kv > 0.0f) || !(pixel_size > 0.0f) ||
+        !(amp_contrast >= 0.0f && amp_contrast <= 1.0f) || !std::isfinite(cs_mm))
+        return GG_ERR_INVALID_ARG;
+    const CtfParams c{voltage_kv, cs_mm, amp_contrast, pixel_size};
+    return launch_ctf(generate ? nullptr : d_cas_images, power, generate ? d_cas_images : nullptr, power,
+                      cas_img_size, n_images, d_defocus, c, (cudaStream_t)stream) == cudaSuccess
+               ? GG_OK
+               : GG_ERR_CUDA;
 }

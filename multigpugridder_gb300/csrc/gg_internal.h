@@ -124,6 +124,20 @@ cudaError_t launch_convert(const float *d_in, void *d_out, int prec, size_t coun
 cudaError_t launch_storage_scale(const float *d_x, size_t count, float target, unsigned int *d_work,
                                  float *d_scale, cudaStream_t s);
 
+// Weak-phase CTF parameters (defocus per image, underfocus positive, Å).
+struct CtfParams {
+    float voltage_kv, cs_mm, amp_contrast, pixel_size; // pixel_size: real-space Å of the N x N images
+};
+// Constants of the CTF kernel: alpha, beta as float pairs, 2 pi in three
+// parts for the reduction, the sin / cos weights.
+struct CtfConsts {
+    float a_hi, a_lo, b_hi, b_lo, p1, p2, p3, inv_2pi, w_sin, w_cos;
+};
+// Over n CAS images of M x M (d_defocus: n defoci in Å): d_mul (optional)
+// *= CTF^mul_power and d_gen (optional) = CTF^gen_power, in one pass.
+cudaError_t launch_ctf(float *d_mul, int mul_power, float *d_gen, int gen_power, int M, int n, const float *d_defocus,
+                       const CtfParams &c, cudaStream_t s);
+
 // Adds to the process-wide count of kernels launched by this library.
 void count_launches(long long n);
 

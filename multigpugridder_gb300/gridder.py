@@ -261,6 +261,28 @@ class MultiGPUGridder:
         self._cas_from_volume = False
         return out
 
+    def reconstructVolCTF(self, images, axes, defocus, voltage_kv=300.0, cs_mm=2.7, amp_contrast=0.1,
+                          pixel_size=1.0):
+        """reconstructVol with each image's weak-phase CTF applied before the
+        back projection (the reference's unimplemented ApplyCTFs flag,
+        src/Gridders/AbstractGridder.h:118-119): the CAS images are multiplied
+        by the CTF and the plane density back-projects CTF^2.  defocus: one
+        value per image in Å (underfocus positive); cs_mm in mm; pixel_size in
+        Å per image pixel."""
+        self.Images = _own(images)
+        self.coordAxes = self._axes(axes)
+        ax = self._axes(self.coordAxes)
+        df = np.ascontiguousarray(defocus, dtype=np.float32).reshape(-1)
+        if df.size != ax.shape[0]:
+            raise ValueError("defocus needs one value per image (%d), got %d" % (ax.shape[0], df.size))
+        n = self.VolumeSize
+        out = np.empty((n, n, n), dtype=np.float32)
+        self._call("gg_reconstruct_volume_ctf", _ptr(ax), ax.shape[0], _ptr(self.Images), _ptr(df),
+                   float(voltage_kv), float(cs_mm), float(amp_contrast), float(pixel_size), _ptr(out))
+        self.Volume = out
+        self._cas_from_volume = False
+        return out
+
     def CheckParameters(self):
         """CheckParameters (MultiGPUGridder_Matlab_Class.m:329-344)."""
         a = np.asarray(self.coordAxes, dtype=np.float64).reshape(-1, 9)

@@ -403,6 +403,41 @@ def reconstruct_vol(imgs, axes, p, precision="f64"):
     return vol_from_cas(cas / (pd + 1e-6), p.N, p.hw, p.interp), cas, pd
 
 
+def electron_wavelength(voltage_kv):
+    """Relativistic electron wavelength in Å at the accelerating voltage:
+    h / sqrt(2 m e U (1 + e U / (2 m c^2))) = 12.2643247 / sqrt(U (1 + 0.978466e-6 U))."""
+    U = float(voltage_kv) * 1e3
+    return 12.2643247 / math.sqrt(U * (1.0 + 0.978466e-6 * U))
+
+
+def ctf_cas(M, defocus, voltage_kv, cs_mm, amp_contrast, pixel_size):
+    """Weak-phase CTF on the CAS-image grid, FP64, shape (n, M, M), DC at
+    (M/2, M/2).  No reference counterpart (the reference declares only the
+    ApplyCTFs flag, src/Gridders/AbstractGridder.h:118-119):
+    CTF = -(sqrt(1 - A^2) sin chi + A cos chi),
+    chi = pi lambda df s^2 - pi/2 Cs lambda^3 s^4, s = |(i, j) - M/2| / (M px)."""
+    lam = electron_wavelength(voltage_kv)
+    f = (np.arange(M) - M // 2) / (M * float(pixel_size))
+    s2 = f[None, :] ** 2 + f[:, None] ** 2
+    df = np.asarray(defocus, dtype=np.float64).reshape(-1, 1, 1)
+    chi = math.pi * lam * df * s2 - 0.5 * math.pi * (cs_mm * 1e7) * lam ** 3 * s2 ** 2
+    A = float(amp_contrast)
+    return -(math.sqrt(1.0 - A * A) * np.sin(chi) + A * np.cos(chi))
+
+
+def reconstruct_vol_ctf(imgs, axes, p, defocus, voltage_kv, cs_mm, amp_contrast, pixel_size, precision="f64"):
+    """reconstructVol with the CTF applied to each CAS image before the back
+    projection and CTF^2 images as the plane density:
+    volFromCAS(BP(CTF . CAS(img)) ./ (BP(CTF^2) + 1e-6))."""
+    c = ctf_cas(p.M, defocus, voltage_kv, cs_mm, amp_contrast, pixel_size)
+    if precision == "f32":
+        c = c.astype(np.float32).astype(np.float64)
+    ci = cas_imgs_from_imgs(imgs, p.M) * c
+    cas = back_project_cas(ci, axes, p, precision)
+    pd = back_project_cas(c * c, axes, p, precision)
+    return vol_from_cas(cas / (pd + 1e-6), p.N, p.hw, p.interp), cas, pd
+
+
 def forward_operator(vol, axes, p):
     """The whole forward operator in FP64, volume -> images (linear in vol)."""
     return forward_project(vol, axes, p, "f64")[0]
