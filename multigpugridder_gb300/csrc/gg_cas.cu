@@ -340,15 +340,17 @@ __global__ void ctf_kernel(float *__restrict__ d_mul, float *__restrict__ d_gen,
         const int di = (int)(r % M) - M / 2, dj = (int)(r / M) - M / 2;
         const float r2 = (float)(di * di + dj * dj);
         const float df = defocus[a];
-        // c = alpha * df as hi + lo
-        const float c_hi = k.a_hi * df;
+        // c = alpha * df as hi + lo (the rounded products are __fmul_rn so
+        // that no FMA contraction changes them: the error terms below assume
+        // each one rounded on its own)
+        const float c_hi = __fmul_rn(k.a_hi, df);
         const float c_lo = fmaf(k.a_hi, df, -c_hi) + k.a_lo * df;
         // t1 = r2 * c
-        const float t1_hi = r2 * c_hi;
+        const float t1_hi = __fmul_rn(r2, c_hi);
         const float t1_lo = fmaf(r2, c_hi, -t1_hi) + r2 * c_lo;
         // t2 = r2^2 * beta
-        const float q_hi = r2 * r2, q_lo = fmaf(r2, r2, -q_hi);
-        const float t2_hi = q_hi * k.b_hi;
+        const float q_hi = __fmul_rn(r2, r2), q_lo = fmaf(r2, r2, -q_hi);
+        const float t2_hi = __fmul_rn(q_hi, k.b_hi);
         const float t2_lo = fmaf(q_hi, k.b_hi, -t2_hi) + q_hi * k.b_lo + q_lo * k.b_hi;
         // chi = t1 - t2 (two-sum of the high parts)
         const float d_hi = t1_hi - t2_hi;
