@@ -450,8 +450,15 @@ void ctf_batch(gg_gridder *h, const float *d_axes, int b, const float *img, cons
     GG_CK(launch_spectrum_to_cas_images(S.spec.p, h->M, b, S.casimg.p, kF32, nullptr, s));
     // CAS images *= CTF, and CTF^2 into S.real (free after the R2C), in one pass
     GG_CK(launch_ctf(S.casimg.p, 1, S.real.p, 2, h->M, b, d_defocus, c, s));
-    bp_batch(h, d_axes, b, nullptr, S.casimg.p, h->cas.p, false, sl, s);
-    bp_batch(h, d_axes, b, nullptr, S.real.p, h->pd.p, false, sl, s);
+    if (h->prec == kF32 && h->bp_mode != GG_BP_ADJOINT) {
+        // both stacks in one back-projection pass
+        ProfScope ps(h, s, GG_KERNEL_BACK);
+        GG_CK(launch_back_project_ref_pair(h->cas.p, h->pd.p, S.casimg.p, S.real.p, h->ker.p, d_axes, b, h->geom(), s));
+        ps.done();
+    } else {
+        bp_batch(h, d_axes, b, nullptr, S.casimg.p, h->cas.p, false, sl, s);
+        bp_batch(h, d_axes, b, nullptr, S.real.p, h->pd.p, false, sl, s);
+    }
 }
 
 void check_ctf(const CtfParams &c)

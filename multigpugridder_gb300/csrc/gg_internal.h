@@ -67,6 +67,12 @@ cudaError_t launch_back_project_ref_density(float *d_vol, float *d_pd, const voi
                                             const float *d_ker, const float *d_axes, int n, const Geom &g,
                                             const float *d_scale, cudaStream_t s);
 
+// Reference-rule back projection of two FP32 image stacks over the same
+// directions in one pass: d_img into d_vol and d_img2 into d_pd, both
+// accumulated, each equal to its own launch_back_project_ref.
+cudaError_t launch_back_project_ref_pair(float *d_vol, float *d_pd, const float *d_img, const float *d_img2,
+                                         const float *d_ker, const float *d_axes, int n, const Geom &g, cudaStream_t s);
+
 // Exact adjoint of launch_forward_project (4 taps), accumulated into d_vol.
 // zero_edges: the KB table's first and last entries are 0 (the fast path
 // relies on it).

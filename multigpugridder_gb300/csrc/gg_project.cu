@@ -369,9 +369,12 @@ __device__ __forceinline__ float ref_pixel_pos(float pi, float pj, float n_x, fl
 // [-2, 2] (checked exhaustively): both round the same exact value once.
 // INSIDE: the whole window lies in the image, so the reference's
 // linear-index test always passes.  Table entry k is read at sker[k * REP].
-template <typename TI, bool ONES, bool DENS, bool INSIDE, int REP = 1>
+// DW: cumW sums img2 * w (a second image back-projected in the same pass,
+// fused as cumSum is) instead of w.
+template <typename TI, bool ONES, bool DENS, bool INSIDE, int REP = 1, bool DW = false>
 __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker, const TI *__restrict__ img_ptr, int M,
-                                           int imgi, int imgj, int imgCenter, float &cumSum, float &cumW)
+                                           int imgi, int imgj, int imgCenter, float &cumSum, float &cumW,
+                                           const float *__restrict__ img2_ptr = nullptr)
 {
 #pragma unroll
     for (int jo = -2; jo <= 2; jo++) {
@@ -392,6 +395,7 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
                 // cumSum += img * w, fused as the reference's build fuses it
                 cumSum = __fmaf_rn(ONES ? 1.0f : ld_f32(img_ptr + lin), w, cumSum);
                 if (DENS) cumW = __fadd_rn(cumW, w);
+                if (DW) cumW = __fmaf_rn(__ldg(img2_ptr + lin), w, cumW);
             }
         }
     }
@@ -450,9 +454,9 @@ struct FootWin {
 // One voxel's WI x WJ window from the footprint (fbase = its top-left pixel,
 // rows FS apart); table entry floor(x) is read at
 // tab + bits(x + 1.5*2^23) * 4 * kTabRep.  Sums row by row, as the reference.
-template <bool DENS, int WI, int WJ, int FS>
+template <bool DENS, int WI, int WJ, int FS, bool DW = false>
 __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase, unsigned tab, float pi0, float pj0,
-                                            float &cumSum, float &cumW)
+                                            float &cumSum, float &cumW, const float *fbase2 = nullptr)
 {
 #pragma unroll
     for (int jo = 0; jo < WJ; jo++) {
@@ -472,6 +476,7 @@ __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase
             w = __fmul_rn(w, lds_f32(tab + b2 * (4u * kTabRep)));
             cumSum = __fmaf_rn(fbase[jo * FS + io], w, cumSum);
             if (DENS) cumW = __fadd_rn(cumW, w);
+            if (DW) cumW = __fmaf_rn(fbase2[jo * FS + io], w, cumW);
         }
     }
 }
@@ -528,13 +533,17 @@ __device__ float adjoint_window_slow(int vi, int vj, int vk, int volCenter, floa
 // every pixel whose forward window misses the voxel gets weight 0, so the
 // wider window adds exact zeros (zero_edges; otherwise the slow path checks
 // window membership as the forward does).
-template <typename TI, bool ONES, bool DENS, bool ADJ>
+// DW (reference rule, FP32 images): pd accumulates the back projection of a
+// second image stack img2 (the same directions) in the same pass, with the
+// same weights and summation order as a separate back projection of img2.
+template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false>
 __global__ void __launch_bounds__(kCThreads, 3)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
                       float kerHW, int bricksX, int bricksY, int tabPad, int zeroEdges,
-                      const float *__restrict__ d_scale)
+                      const float *__restrict__ d_scale, const float *__restrict__ img2)
 {
+    static_assert(!DW || (!ONES && !DENS && !ADJ), "the second image stack is a reference-rule option");
     constexpr int W = ADJ ? 7 : 5, HALF = W / 2;
     constexpr int FW = ADJ ? 24 : kFootW, FH = FW, FS = FW + 1;
     extern __shared__ float stab[]; // (kerSize + 2 tabPad) entries x kTabRep copies
@@ -545,8 +554,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     // per-voxel sums [warp][block voxel]; a voxel is updated by at most one
     // lane per direction, directions in order, so no atomics are needed
     __shared__ float sacc[kCThreads / 32 * kWarpVox];
-    __shared__ float saccw[DENS ? kCThreads / 32 * kWarpVox : 1];
+    __shared__ float saccw[DENS || DW ? kCThreads / 32 * kWarpVox : 1];
     __shared__ float sfoot[kCThreads / 32 * FH * FS];
+    __shared__ float sfoot2[DW ? kCThreads / 32 * FH * FS : 1];
     __shared__ unsigned char svox[kCThreads / 32 * kWarpVox];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -571,9 +581,10 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     const unsigned tab = (unsigned)__cvta_generic_to_shared(stab) + 4u * (unsigned)(lane % kTabRep) +
                          4u * kTabRep * ((unsigned)tabPad - 0x4B400000u);
     float *wfoot = sfoot + warp * (FH * FS);
+    float *wfoot2 = sfoot2 + (DW ? warp * (FH * FS) : 0);
     unsigned char *wvox = svox + warp * kWarpVox;
     float *wacc = sacc + warp * kWarpVox;
-    float *waccw = saccw + (DENS ? warp * kWarpVox : 0);
+    float *waccw = saccw + (DENS || DW ? warp * kWarpVox : 0);
 
     // this lane's voxels: x = lx, y = ly, z = bz + s
     const int lx = bx + (lane & 7), ly = by + (lane >> 3);
@@ -587,7 +598,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                              (long long)(lz - volCenter) * (lz - volCenter);
         if (lx < V && ly < V && lz < V && d2 <= reach2) inmask |= 1u << s;
         wacc[lane + 32 * s] = 0.0f;
-        if (DENS) waccw[lane + 32 * s] = 0.0f;
+        if (DENS || DW) waccw[lane + 32 * s] = 0.0f;
     }
     const float kerCenter = ((float)kerSize - 1) / 2;
     const float kerScale = kerCenter / kerHW;
@@ -677,6 +688,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             const float nx0 = ax[0], nx1 = ax[1], nx2 = ax[2];
             const float ny0 = ax[3], ny1 = ax[4], ny2 = ax[5];
             const TI *img_ptr = img + (size_t)(c0 + al) * MM;
+            const float *img2_ptr = DW ? img2 + (size_t)(c0 + al) * MM : nullptr;
 
             // this warp's footprint (uniform across the warp)
             int fi0 = 0, fj0 = 0, fh = 0;
@@ -696,9 +708,13 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                     const int c = lane & (kFootW - 1);
                     for (int r = lane >> 4; r < fh; r += 2) {
                         const int lin = (fj0 + r) * M + (fi0 + c);
-                        float v = 0.0f;
-                        if (lin >= 0 && lin < MM) v = ONES ? 1.0f : ld_f32(img_ptr + lin);
+                        float v = 0.0f, v2 = 0.0f;
+                        if (lin >= 0 && lin < MM) {
+                            v = ONES ? 1.0f : ld_f32(img_ptr + lin);
+                            if (DW) v2 = __ldg(img2_ptr + lin);
+                        }
                         wfoot[r * FS + c] = v;
+                        if (DW) wfoot2[r * FS + c] = v2;
                     }
                 } else if (foot) {
                     // the forward projection's pixels: inside the image and the mask
@@ -736,7 +752,8 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                            kerCenterHalf - (float)vk * sg};
                         const float *fb = wfoot + rj * FS + ri;
                         const float pi0 = (float)(imgi - HALF - imgCenter), pj0 = (float)(imgj - HALF - imgCenter);
-                        foot_window<DENS, W, W, FS>(fwin, fb, tab, pi0, pj0, cs, cw);
+                        foot_window<DENS, W, W, FS, DW>(fwin, fb, tab, pi0, pj0, cs, cw,
+                                                        DW ? wfoot2 + rj * FS + ri : nullptr);
                     } else if (ADJ) {
                         cs = adjoint_window_slow<TI>(vi, vj, vk, volCenter, nx0, nx1, nx2, ny0, ny1, ny2, img_ptr, M,
                                                      imgCenter, maskR, sker, kerScale, kerCenterHalf, kerSize);
@@ -744,13 +761,15 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                         const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk,
                                            (float)volCenter, kerScale, kerCenterHalf};
                         if (inside)
-                            ref_window<TI, ONES, DENS, true, kTabRep>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cs, cw);
+                            ref_window<TI, ONES, DENS, true, kTabRep, DW>(rw, sker, img_ptr, M, imgi, imgj, imgCenter,
+                                                                          cs, cw, img2_ptr);
                         else
-                            ref_window<TI, ONES, DENS, false, kTabRep>(rw, sker, img_ptr, M, imgi, imgj, imgCenter, cs, cw);
+                            ref_window<TI, ONES, DENS, false, kTabRep, DW>(rw, sker, img_ptr, M, imgi, imgj, imgCenter,
+                                                                           cs, cw, img2_ptr);
                     }
                     // cumSumAllAxes += cumSum (gpuBackProject.cu:106), in direction order
                     wacc[l] = __fadd_rn(wacc[l], cs);
-                    if (DENS) waccw[l] = __fadd_rn(waccw[l], cw);
+                    if (DENS || DW) waccw[l] = __fadd_rn(waccw[l], cw);
                 }
             }
             __syncwarp();  // the next direction rewrites the list, the footprint and these sums
@@ -763,25 +782,25 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         if (!((inmask >> s) & 1u)) continue;
         const size_t o = (size_t)(bz + s) * V * V + (size_t)ly * V + lx;
         vol[o] = vol[o] + wacc[lane + 32 * s] * sc;
-        if (DENS) pd[o] = pd[o] + waccw[lane + 32 * s];
+        if (DENS || DW) pd[o] = pd[o] + waccw[lane + 32 * s];
     }
 }
 
-template <typename TI, bool ONES, bool DENS = false, bool ADJ = false>
+template <typename TI, bool ONES, bool DENS = false, bool ADJ = false, bool DW = false>
 static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
                                        const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr,
-                                       bool zero_edges = true)
+                                       bool zero_edges = true, const float *img2 = nullptr)
 {
     if (n <= 0) return cudaSuccess;
     const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
     const long long nb = (long long)bx * by * bz;
     const int pad = bp_table_pad(g.ker_size, ADJ);
     const size_t dyn = (size_t)(g.ker_size + 2 * pad) * kTabRep * sizeof(float);
-    auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ>;
+    auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
     kern<<<(unsigned)nb, kCThreads, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
-                                              g.ker_hw, bx, by, pad, zero_edges ? 1 : 0, scale);
+                                              g.ker_hw, bx, by, pad, zero_edges ? 1 : 0, scale, img2);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -804,6 +823,13 @@ cudaError_t launch_back_project_ref_density(float *d_vol, float *d_pd, const voi
         return launch_bp_compact_t<__half, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
     return launch_bp_compact_t<__nv_bfloat16, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g,
                                                            scale, s, d_pd);
+}
+
+cudaError_t launch_back_project_ref_pair(float *d_vol, float *d_pd, const float *d_img, const float *d_img2,
+                                         const float *d_ker, const float *d_axes, int n, const Geom &g, cudaStream_t s)
+{
+    return launch_bp_compact_t<float, false, false, false, true>(d_vol, d_img, d_ker, d_axes, n, g, nullptr, s, d_pd,
+                                                                  true, d_img2);
 }
 
 cudaError_t launch_back_project_adjoint(float *d_vol, const void *d_img, int iprec, const float *d_ker,

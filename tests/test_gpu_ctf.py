@@ -78,7 +78,10 @@ def _data(N, n, seed):
 
 
 def test_ctf_reconstruction_without_aberration_is_minus_plain(cuda):
-    """defocus 0, Cs 0, A = 1: CTF = -1 at every pixel and CTF^2 = 1."""
+    """defocus 0, Cs 0, A = 1: CTF = -1 at every pixel and CTF^2 = 1, so the
+    one-pass back projection of (CTF . image, CTF^2) must give minus the
+    plain reconstruction bit for bit (negation is exact and 1 * w + s rounds
+    as w + s)."""
     import multigpugridder_gb300 as gg
 
     N = 32
@@ -88,7 +91,7 @@ def test_ctf_reconstruction_without_aberration_is_minus_plain(cuda):
         imgs = g.forwardProject(axes)
         plain = g.reconstructVol(imgs, axes)
         ctf = g.reconstructVolCTF(imgs, axes, np.zeros(len(axes)), KV, 0.0, 1.0, 1.0)
-    assert O.rel_l2(ctf, -plain) < 1e-6
+    assert np.array_equal(ctf, -plain)
 
 
 @pytest.mark.parametrize("N", [16, 32])
@@ -106,6 +109,25 @@ def test_ctf_reconstruction_matches_oracle(cuda, N):
     ref = O.reconstruct_vol_ctf(imgs, axes, p, df, KV, CS, AMP, px, precision="f32")[0]
     assert np.all(np.isfinite(rec))
     assert O.rel_l2(rec, ref) < TOL
+
+
+@pytest.mark.parametrize("prec", ["bf16", "f16"])
+def test_ctf_reconstruction_reduced_precision(cuda, prec):
+    """FP16 / BF16 storage: the two stacks take separate back projections;
+    the result stays within 1e-3 relative L2 of the FP64 oracle."""
+    import multigpugridder_gb300 as gg
+
+    N = 32
+    p = O.Params(N)
+    vol, axes = _data(N, 30, 70)
+    df = np.random.default_rng(7).uniform(5000.0, 25000.0, len(axes)).astype(np.float32)
+    with gg.MultiGPUGridder(N, len(axes), adjustInterpFactor=False) as g:
+        g.setVolume(vol)
+        imgs = g.forwardProject(axes)
+        g.set_precision(prec)
+        rec = g.reconstructVolCTF(imgs, axes, df, KV, CS, AMP, 2.0)
+    ref = O.reconstruct_vol_ctf(imgs, axes, p, df, KV, CS, AMP, 2.0)[0]
+    assert O.rel_l2(rec, ref) < 1e-3
 
 
 def test_ctf_reconstruction_device_form_equals_host_form(cuda):
