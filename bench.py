@@ -57,6 +57,7 @@ def parse():
                     help="requests in the closed-loop served vs sequential plain-path comparison")
     ap.add_argument("--no-precision", action="store_true", help="skip the 256^3 storage-precision comparison")
     ap.add_argument("--no-autograd", action="store_true", help="skip the gradient-descent timing")
+    ap.add_argument("--no-ctf", action="store_true", help="skip the CTF-corrected reconstruction timing")
     return ap.parse_args()
 
 
@@ -295,13 +296,15 @@ def run_gb300(args):
                 "sample": "%d of %d directions timed, step extrapolated (t_fixed + D/S * t_sample)" % (S, n)}
 
     g.close()
-    serve = prec = grad = None
+    serve = prec = grad = ctf = None
     if rank == 0 and world == 1 and args.serve_seconds > 0:
         serve = run_serve(args)
     if rank == 0 and world == 1 and not args.no_precision and args.size == 128:
         prec = run_precision(args)
     if rank == 0 and world == 1 and not args.no_autograd and args.size == 128:
         grad = run_autograd(args)
+    if rank == 0 and world == 1 and not args.no_ctf:
+        ctf = run_ctf(args, vol, axes)
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -314,7 +317,8 @@ def run_gb300(args):
                           "l2": "inputs larger than L2 (10,000 images = %d MB per step) and an untimed %d MB "
                                 "write between steps" % (n * N * N * 4 >> 20, flush.numel() * 4 >> 20)},
                "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
-               "clocks": clk, "step_ms": ms_steps, "serve": serve, "precision": prec, "autograd": grad}
+               "clocks": clk, "step_ms": ms_steps, "serve": serve, "precision": prec, "autograd": grad,
+               "ctf": ctf}
         print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -572,6 +576,54 @@ def run_autograd(args):
                         "||P(V) - Y||^2 (Y = P(V_true) + noise at SNR 0.1), 20 gradient-descent iterations",
             "ms_per_iteration": ms, "directions_per_s": B / (ms / 1e3),
             "loss_first_cycle": sum(first), "loss_last_cycle": sum(last)}
+
+
+# ---- CTF application before back projection ------------------------------------
+def run_ctf(args, vol, axes):
+    """reconstructVol of the step's images with and without the CTF applied
+    before the back projection (device pointers, FP32): defoci uniform in
+    8,000-25,000 Å, 300 kV, Cs 2.7 mm, amplitude contrast 0.1, 1 Å pixels."""
+    import torch
+
+    from multigpugridder_gb300 import MultiGPUGridder
+    from multigpugridder_gb300._lib import check, lib
+
+    L = lib()
+    N, n = args.size, len(axes)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    g = MultiGPUGridder(N, n, 2.0, MaxAxesToAllocate=args.batch)
+    h = g.handle
+    s = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(s.cuda_stream)
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    d_vol = torch.from_numpy(vol).to(dev)
+    d_ax = torch.from_numpy(axes).to(dev)
+    d_img = torch.empty((n, N, N), device=dev)
+    d_out = torch.empty((N, N, N), device=dev)
+    df = torch.from_numpy(np.random.default_rng(9).uniform(8000.0, 25000.0, n).astype(np.float32)).to(dev)
+    check(L.gg_set_volume_dev(h, vp(d_vol), sp), h)
+    check(L.gg_forward_project_dev(h, vp(d_ax), n, vp(d_img), None, sp), h)
+    calls = {"plain": lambda: check(L.gg_reconstruct_volume_dev(h, vp(d_ax), n, vp(d_img), vp(d_out), sp), h),
+             "ctf": lambda: check(L.gg_reconstruct_volume_ctf_dev(h, vp(d_ax), n, vp(d_img), vp(df), 300.0, 2.7, 0.1,
+                                                                  1.0, vp(d_out), sp), h)}
+    res = {}
+    for name, call in calls.items():
+        for _ in range(max(3, args.warmup)):
+            call()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(s)
+        for _ in range(args.steps):
+            call()
+        b.record(s)
+        torch.cuda.synchronize()
+        res[name + "_ms"] = a.elapsed_time(b) / args.steps
+    res["finite"] = bool(torch.isfinite(d_out).all())
+    g.close()
+    res["ctf_over_plain"] = res["ctf_ms"] / res["plain_ms"]
+    res["workload"] = ("reconstructVol of %d images %d^2 (interpFactor 2), FP32, device pointers; CTF: defoci "
+                       "8,000-25,000 Å, 300 kV, Cs 2.7 mm, A 0.1, 1 Å pixels" % (n, N))
+    return res
 
 
 def run_e2e(args, g, vol, axes, world):
