@@ -572,23 +572,25 @@ void fp_host(gg_gridder *h, const float *axes, int n, float *images_out, float *
 
 // Back projection with host inputs: batch c is copied in on the copy stream
 // (staged when pageable) while batch c-1 is transformed and back-projected.
-void bp_host(gg_gridder *h, const float *axes, int n, const float *images, const float *casimgs, float *target,
-             bool ones, float *pd = nullptr)
+// Host input pipeline, double-buffered: batch c's inputs (b * per floats from
+// `src`) are copied into slot c&1 on the copy stream (through pinned staging
+// when `src` is pageable) while batch c-1 computes; compute(a0, b, sl, dbuf)
+// then enqueues the batch's work on the compute stream.  src = NULL uploads
+// nothing.  casimg_slot: the inputs land in the slot's CAS-image buffer
+// instead of its image buffer.
+template <typename F>
+void host_batches(gg_gridder *h, int n, const float *src, size_t per, bool casimg_slot, F compute)
 {
     cudaStream_t cs = h->cs, cp = h->cp;
-    upload_axes(h, axes, n, cs);
     const int B = h->max_batch;
-    const size_t MM = (size_t)h->M * h->M, NN = (size_t)h->N * h->N;
-    const float *src = casimgs ? casimgs : images;
-    const size_t per = casimgs ? MM : NN;
     const bool pinned = src && host_is_pinned(src);
     const int nb = (n + B - 1) / B;
     for (int c = 0; c < nb; c++) {
         const int sl = c & 1, a0 = c * B, b = std::min(B, n - a0);
         auto &S = h->slot[sl];
         ensure_slot(h, sl, B, true);
-        float *dbuf = casimgs ? S.casimg.p : S.img.p;
-        if (!ones) {
+        float *dbuf = casimg_slot ? S.casimg.p : S.img.p;
+        if (src) {
             // the slot's buffers are free once its previous batch finished computing
             GG_CK(cudaStreamWaitEvent(cp, S.ev_ready, 0));
             const float *hsrc = src + (size_t)a0 * per;
@@ -602,12 +604,23 @@ void bp_host(gg_gridder *h, const float *axes, int n, const float *images, const
             GG_CK(cudaEventRecord(S.ev_free, cp));
             GG_CK(cudaStreamWaitEvent(cs, S.ev_free, 0));
         }
-        bp_batch(h, h->axes.p + (size_t)a0 * 9, b, casimgs ? nullptr : dbuf, casimgs ? dbuf : nullptr, target, ones, sl,
-                 cs, pd);
+        compute(a0, b, sl, dbuf);
         GG_CK(cudaEventRecord(S.ev_ready, cs));
     }
     GG_CK(cudaStreamSynchronize(cs));
     GG_CK(cudaStreamSynchronize(cp));
+}
+
+void bp_host(gg_gridder *h, const float *axes, int n, const float *images, const float *casimgs, float *target,
+             bool ones, float *pd = nullptr)
+{
+    upload_axes(h, axes, n, h->cs);
+    const size_t MM = (size_t)h->M * h->M, NN = (size_t)h->N * h->N;
+    const float *src = ones ? nullptr : (casimgs ? casimgs : images);
+    host_batches(h, n, src, casimgs ? MM : NN, casimgs != nullptr, [&](int a0, int b, int sl, float *dbuf) {
+        bp_batch(h, h->axes.p + (size_t)a0 * 9, b, casimgs ? nullptr : dbuf, casimgs ? dbuf : nullptr, target, ones,
+                 sl, h->cs, pd);
+    });
 }
 
 void init_handle(gg_gridder *h)
@@ -1166,15 +1179,10 @@ extern "C" int gg_reconstruct_volume_ctf(gg_gridder *h, const float *axes, int n
         h->pd.ensure(V3);
         GG_CK(cudaMemsetAsync(h->cas.p, 0, V3 * sizeof(float), s));
         GG_CK(cudaMemsetAsync(h->pd.p, 0, V3 * sizeof(float), s));
-        const int B = h->max_batch;
-        for (int a0 = 0; a0 < n_axes; a0 += B) {
-            const int b = std::min(B, n_axes - a0);
-            ensure_slot(h, 0, B, true);
-            auto &S = h->slot[0];
-            GG_CK(cudaMemcpyAsync(S.img.p, images + (size_t)a0 * NN, (size_t)b * NN * sizeof(float),
-                                  cudaMemcpyHostToDevice, s));
-            ctf_batch(h, h->axes.p + (size_t)a0 * 9, b, S.img.p, df.p + a0, c, 0, s);
-        }
+        if (n_axes > 0)
+            host_batches(h, n_axes, images, NN, false, [&](int a0, int b, int sl, float *dbuf) {
+                ctf_batch(h, h->axes.p + (size_t)a0 * 9, b, dbuf, df.p + a0, c, sl, s);
+            });
         GG_CK(launch_divide_plane_density(h->cas.p, h->pd.p, V3, 1e-6f, s));
         h->vol_io.ensure(N3);
         do_get_volume(h, h->cas.p, h->vol_io.p, s);
