@@ -121,87 +121,150 @@ __global__ void fft_output_to_vol_kernel(const float *__restrict__ y, int M, int
 
 // ---- 2-D: CAS images -> images (forward-projection output path) -----------
 
-__global__ void cas_images_to_spectrum_kernel(const float *__restrict__ cas, int M, int n, cufftComplex *__restrict__ spec)
+// Per-image row kernels: a (kRowX, kRowY) block covers kRowY rows of one
+// image, blockIdx.y walks the images; each thread takes kRowU columns kRowX
+// apart per chunk and issues its loads before its stores (more bytes in
+// flight than one element per thread, and no per-element division).
+constexpr int kRowX = 64, kRowY = 4, kRowU = 4;
+
+static inline dim3 row_grid(int rows, int n)
+{
+    return dim3((unsigned)((rows + kRowY - 1) / kRowY), (unsigned)(n < 65535 ? n : 65535));
+}
+
+__global__ void __launch_bounds__(kRowX *kRowY)
+cas_images_to_spectrum_kernel(const float *__restrict__ cas, int M, int n, cufftComplex *__restrict__ spec)
 {
     const int H = M / 2 + 1;
-    const size_t per = (size_t)M * H;
-    const size_t total = per * n;
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-        const size_t a = e / per;
-        const int rem = (int)(e - a * per);
-        const int u = rem % H, v = rem / H;
-        const int i = shift_idx(u, M), j = shift_idx(v, M);
-        cufftComplex c;
-        c.x = 0.0f;
-        c.y = 0.0f;
-        if (i != 0 && j != 0) {
-            const float *img = cas + a * M * M;
-            const float r1 = img[(size_t)j * M + i];
-            const float r2 = img[(size_t)(M - j) * M + (M - i)];
-            c.x = 0.5f * (r1 + r2);
-            c.y = 0.5f * (r1 - r2);
+    const int v = blockIdx.x * kRowY + threadIdx.y;
+    if (v >= M) return;
+    const int j = shift_idx(v, M);
+    for (int a = blockIdx.y; a < n; a += gridDim.y) {
+        const float *img = cas + (size_t)a * M * M;
+        const float *r1 = img + (size_t)j * M, *r2 = img + (size_t)(M - j) * M;
+        cufftComplex *out = spec + ((size_t)a * M + v) * H;
+        for (int u0 = threadIdx.x; u0 < H; u0 += kRowX * kRowU) {
+            float x1[kRowU], x2[kRowU];
+#pragma unroll
+            for (int k = 0; k < kRowU; k++) {
+                const int u = u0 + k * kRowX;
+                const int i = u < H ? shift_idx(u, M) : 0;
+                const bool live = u < H && i != 0 && j != 0;
+                x1[k] = live ? __ldg(r1 + i) : 0.0f;
+                x2[k] = live ? __ldg(r2 + (M - i)) : 0.0f;
+            }
+#pragma unroll
+            for (int k = 0; k < kRowU; k++) {
+                const int u = u0 + k * kRowX;
+                if (u < H) {
+                    cufftComplex c;
+                    c.x = 0.5f * (x1[k] + x2[k]);
+                    c.y = 0.5f * (x1[k] - x2[k]);
+                    out[u] = c;
+                }
+            }
         }
-        spec[e] = c;
     }
 }
 
-__global__ void fft_output_to_images_kernel(const float *__restrict__ y, int M, int N, int n, float *__restrict__ img)
+__global__ void __launch_bounds__(kRowX *kRowY)
+fft_output_to_images_kernel(const float *__restrict__ y, int M, int N, int n, float *__restrict__ img)
 {
-    const size_t per = (size_t)N * N;
-    const size_t total = per * n;
     const int ob = (M - N) / 2;
     const float scale = 1.0f / ((float)M * (float)M);
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-        const size_t a = e / per;
-        const int rem = (int)(e - a * per);
-        const int oi = rem % N, oj = rem / N;
-        const int i = shift_idx(oi + ob, M), j = shift_idx(oj + ob, M);
-        img[e] = y[a * M * M + (size_t)j * M + i] * scale;
+    const int oj = blockIdx.x * kRowY + threadIdx.y;
+    if (oj >= N) return;
+    const int j = shift_idx(oj + ob, M);
+    for (int a = blockIdx.y; a < n; a += gridDim.y) {
+        const float *yr = y + ((size_t)a * M + j) * M;
+        float *ir = img + ((size_t)a * N + oj) * N;
+        for (int o0 = threadIdx.x; o0 < N; o0 += kRowX * kRowU) {
+            float v[kRowU];
+#pragma unroll
+            for (int k = 0; k < kRowU; k++) {
+                const int oi = o0 + k * kRowX;
+                v[k] = oi < N ? __ldg(yr + shift_idx(oi + ob, M)) : 0.0f;
+            }
+#pragma unroll
+            for (int k = 0; k < kRowU; k++) {
+                const int oi = o0 + k * kRowX;
+                if (oi < N) ir[oi] = v[k] * scale;
+            }
+        }
     }
 }
 
 // ---- 2-D: images -> CAS images (back-projection input path) --------------
 
-__global__ void images_to_fft_input_kernel(const float *__restrict__ img, int N, int M, int n, float *__restrict__ x)
+__global__ void __launch_bounds__(kRowX *kRowY)
+images_to_fft_input_kernel(const float *__restrict__ img, int N, int M, int n, float *__restrict__ x)
 {
-    const size_t per = (size_t)M * M;
-    const size_t total = per * n;
     const int b = (M - N) / 2;
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-        const size_t a = e / per;
-        const int rem = (int)(e - a * per);
-        const int qi = rem % M, qj = rem / M;
-        const int oi = shift_idx(qi, M) - b, oj = shift_idx(qj, M) - b;
-        float v = 0.0f;
-        if ((unsigned)oi < (unsigned)N && (unsigned)oj < (unsigned)N) v = img[a * N * N + (size_t)oj * N + oi];
-        x[e] = v;
+    const int qj = blockIdx.x * kRowY + threadIdx.y;
+    if (qj >= M) return;
+    const int oj = shift_idx(qj, M) - b;
+    const bool row_in = (unsigned)oj < (unsigned)N;
+    for (int a = blockIdx.y; a < n; a += gridDim.y) {
+        const float *ir = img + ((size_t)a * N + (row_in ? oj : 0)) * N;
+        float *xr = x + ((size_t)a * M + qj) * M;
+        for (int q0 = threadIdx.x; q0 < M; q0 += kRowX * kRowU) {
+            float v[kRowU];
+#pragma unroll
+            for (int k = 0; k < kRowU; k++) {
+                const int qi = q0 + k * kRowX;
+                const int oi = qi < M ? shift_idx(qi, M) - b : -1;
+                v[k] = row_in && (unsigned)oi < (unsigned)N ? __ldg(ir + oi) : 0.0f;
+            }
+#pragma unroll
+            for (int k = 0; k < kRowU; k++) {
+                const int qi = q0 + k * kRowX;
+                if (qi < M) xr[qi] = v[k];
+            }
+        }
     }
 }
 
-template <typename T>
-__global__ void spectrum_to_cas_images_kernel(const cufftComplex *__restrict__ spec, int M, int n, T *__restrict__ cas,
-                                              const float *__restrict__ d_scale)
+// Row j of CAS image a from the half spectrum: Re+Im at (u, v) = the shifted
+// (i, j) for u <= M/2, else Re-Im at the Hermitian mirror.  ADJ: the adjoint
+// form (first row and column zero, times `post`).
+template <typename T, bool ADJ>
+__global__ void __launch_bounds__(kRowX *kRowY)
+spectrum_to_cas_images_kernel(const cufftComplex *__restrict__ spec, int M, int n, T *__restrict__ cas,
+                              const float *__restrict__ d_scale, float post)
 {
-    const float inv_scale = d_scale ? 1.0f / *d_scale : 1.0f;
+    const float mul = ADJ ? post : (d_scale ? 1.0f / *d_scale : 1.0f);
     const int H = M / 2 + 1;
-    const size_t per = (size_t)M * M;
-    const size_t total = per * n;
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-        const size_t a = e / per;
-        const int rem = (int)(e - a * per);
-        const int i = rem % M, j = rem / M;
-        const int u = shift_idx(i, M), v = shift_idx(j, M);
-        const cufftComplex *s = spec + a * (size_t)M * H;
-        float out;
-        if (u <= M / 2) {
-            const cufftComplex c = s[(size_t)v * H + u];
-            out = c.x + c.y;
-        } else {
-            const int v2 = v ? M - v : 0;
-            const cufftComplex c = s[(size_t)v2 * H + (M - u)];
-            out = c.x - c.y;
+    const int j = blockIdx.x * kRowY + threadIdx.y;
+    if (j >= M) return;
+    const int v = shift_idx(j, M), v2 = v ? M - v : 0;
+    for (int a = blockIdx.y; a < n; a += gridDim.y) {
+        const cufftComplex *s = spec + (size_t)a * M * H;
+        const cufftComplex *r1 = s + (size_t)v * H, *r2 = s + (size_t)v2 * H;
+        T *cr = cas + ((size_t)a * M + j) * M;
+        for (int i0 = threadIdx.x; i0 < M; i0 += kRowX * kRowU) {
+            float o[kRowU];
+#pragma unroll
+            for (int k = 0; k < kRowU; k++) {
+                const int i = i0 + k * kRowX;
+                float out = 0.0f;
+                if (i < M && (!ADJ || (i != 0 && j != 0))) {
+                    const int u = shift_idx(i, M);
+                    if (u <= M / 2) {
+                        const cufftComplex c = r1[u];
+                        out = c.x + c.y;
+                    } else {
+                        const cufftComplex c = r2[M - u];
+                        out = c.x - c.y;
+                    }
+                }
+                o[k] = out;
+            }
+#pragma unroll
+            for (int k = 0; k < kRowU; k++) {
+                const int i = i0 + k * kRowX;
+                if (i < M) cr[i] = from_f32<T>(o[k] * mul);
+            }
         }
-        cas[e] = from_f32<T>(out * inv_scale);
     }
 }
 
@@ -209,34 +272,7 @@ __global__ void spectrum_to_cas_images_kernel(const cufftComplex *__restrict__ s
 // Gradient of images -> CAS images: the adjoint of (FromCAS, shift, inverse
 // FFT / M^2, shift, real part, crop).  For the FFT of a real image FromCAS^T
 // equals Re+Im, so this is spectrum_to_cas_images with the first row and
-// column (zeroed by FromCAS) dropped and the 1/M^2 applied.
-__global__ void spectrum_to_cas_images_adjoint_kernel(const cufftComplex *__restrict__ spec, int M, int n,
-                                                      float *__restrict__ cas)
-{
-    const int H = M / 2 + 1;
-    const size_t per = (size_t)M * M;
-    const size_t total = per * n;
-    const float scale = 1.0f / ((float)M * (float)M);
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-        const size_t a = e / per;
-        const int rem = (int)(e - a * per);
-        const int i = rem % M, j = rem / M;
-        float out = 0.0f;
-        if (i != 0 && j != 0) {
-            const int u = shift_idx(i, M), v = shift_idx(j, M);
-            const cufftComplex *s = spec + a * (size_t)M * H;
-            if (u <= M / 2) {
-                const cufftComplex c = s[(size_t)v * H + u];
-                out = c.x + c.y;
-            } else {
-                const int v2 = v ? M - v : 0;
-                const cufftComplex c = s[(size_t)v2 * H + (M - u)];
-                out = c.x - c.y;
-            }
-        }
-        cas[e] = out * scale;
-    }
-}
+// column (zeroed by FromCAS) dropped and the 1/M^2 applied (the ADJ form).
 
 // Gradient of the CAS volume -> volume, first half: crop V^3 to the inner M^3
 // and fftshift (the adjoint of the zero-pad and of the output fftshift).
@@ -331,41 +367,46 @@ __global__ void transpose_volume_kernel(const float *__restrict__ in, int V, flo
 // first two short enough that k * part is exact); sincosf then sees |r| <= pi.
 // A real, even CTF multiplies Re and Im alike, so it applies to CAS images
 // directly.  d_mul (optional) *= CTF^mul_power; d_gen (optional) = CTF^gen_power.
-__global__ void ctf_kernel(float *__restrict__ d_mul, float *__restrict__ d_gen, int M, int n,
-                           const float *__restrict__ defocus, CtfConsts k, int mul_power, int gen_power)
+__global__ void __launch_bounds__(kRowX *kRowY)
+ctf_kernel(float *__restrict__ d_mul, float *__restrict__ d_gen, int M, int n, const float *__restrict__ defocus,
+           CtfConsts k, int mul_power, int gen_power)
 {
-    const size_t MM = (size_t)M * M, total = MM * n;
-    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-        const size_t a = e / MM, r = e - a * MM;
-        const int di = (int)(r % M) - M / 2, dj = (int)(r / M) - M / 2;
-        const float r2 = (float)(di * di + dj * dj);
+    const int j = blockIdx.x * kRowY + threadIdx.y;
+    if (j >= M) return;
+    const int dj = j - M / 2;
+    for (int a = blockIdx.y; a < n; a += gridDim.y) {
         const float df = defocus[a];
         // c = alpha * df as hi + lo (the rounded products are __fmul_rn so
         // that no FMA contraction changes them: the error terms below assume
         // each one rounded on its own)
         const float c_hi = __fmul_rn(k.a_hi, df);
         const float c_lo = fmaf(k.a_hi, df, -c_hi) + k.a_lo * df;
-        // t1 = r2 * c
-        const float t1_hi = __fmul_rn(r2, c_hi);
-        const float t1_lo = fmaf(r2, c_hi, -t1_hi) + r2 * c_lo;
-        // t2 = r2^2 * beta
-        const float q_hi = __fmul_rn(r2, r2), q_lo = fmaf(r2, r2, -q_hi);
-        const float t2_hi = __fmul_rn(q_hi, k.b_hi);
-        const float t2_lo = fmaf(q_hi, k.b_hi, -t2_hi) + q_hi * k.b_lo + q_lo * k.b_hi;
-        // chi = t1 - t2 (two-sum of the high parts)
-        const float d_hi = t1_hi - t2_hi;
-        const float bb = d_hi - t1_hi, aa = d_hi - bb;
-        const float d_lo = ((t1_hi - aa) + (-t2_hi - bb)) + (t1_lo - t2_lo);
-        // reduction mod 2 pi
-        const float kk = rintf(d_hi * k.inv_2pi);
-        float red = fmaf(-kk, k.p1, d_hi);
-        red = fmaf(-kk, k.p2, red);
-        red = fmaf(-kk, k.p3, red) + d_lo;
-        float sn, cs;
-        sincosf(red, &sn, &cs);
-        const float ctf = -(k.w_sin * sn + k.w_cos * cs);
-        if (d_mul) d_mul[e] *= mul_power == 2 ? ctf * ctf : ctf;
-        if (d_gen) d_gen[e] = gen_power == 2 ? ctf * ctf : ctf;
+        const size_t row = ((size_t)a * M + j) * M;
+        for (int i = threadIdx.x; i < M; i += kRowX) {
+            const int di = i - M / 2;
+            const float r2 = (float)(di * di + dj * dj);
+            // t1 = r2 * c
+            const float t1_hi = __fmul_rn(r2, c_hi);
+            const float t1_lo = fmaf(r2, c_hi, -t1_hi) + r2 * c_lo;
+            // t2 = r2^2 * beta
+            const float q_hi = __fmul_rn(r2, r2), q_lo = fmaf(r2, r2, -q_hi);
+            const float t2_hi = __fmul_rn(q_hi, k.b_hi);
+            const float t2_lo = fmaf(q_hi, k.b_hi, -t2_hi) + q_hi * k.b_lo + q_lo * k.b_hi;
+            // chi = t1 - t2 (two-sum of the high parts)
+            const float d_hi = t1_hi - t2_hi;
+            const float bb = d_hi - t1_hi, aa = d_hi - bb;
+            const float d_lo = ((t1_hi - aa) + (-t2_hi - bb)) + (t1_lo - t2_lo);
+            // reduction mod 2 pi
+            const float kk = rintf(d_hi * k.inv_2pi);
+            float red = fmaf(-kk, k.p1, d_hi);
+            red = fmaf(-kk, k.p2, red);
+            red = fmaf(-kk, k.p3, red) + d_lo;
+            float sn, cs;
+            sincosf(red, &sn, &cs);
+            const float ctf = -(k.w_sin * sn + k.w_cos * cs);
+            if (d_mul) d_mul[row + i] *= mul_power == 2 ? ctf * ctf : ctf;
+            if (d_gen) d_gen[row + i] = gen_power == 2 ? ctf * ctf : ctf;
+        }
     }
 }
 
@@ -428,7 +469,7 @@ cudaError_t launch_fft_output_to_vol(const float *d_y, int M, int N, const doubl
 cudaError_t launch_cas_images_to_spectrum(const float *d_cas, int M, int n, cufftComplex *d_spec, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    cas_images_to_spectrum_kernel<<<grid_for((size_t)M * (M / 2 + 1) * n, kT), kT, 0, s>>>(d_cas, M, n, d_spec);
+    cas_images_to_spectrum_kernel<<<row_grid(M, n), dim3(kRowX, kRowY), 0, s>>>(d_cas, M, n, d_spec);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -436,7 +477,7 @@ cudaError_t launch_cas_images_to_spectrum(const float *d_cas, int M, int n, cuff
 cudaError_t launch_fft_output_to_images(const float *d_y, int M, int N, int n, float *d_img, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    fft_output_to_images_kernel<<<grid_for((size_t)N * N * n, kT), kT, 0, s>>>(d_y, M, N, n, d_img);
+    fft_output_to_images_kernel<<<row_grid(N, n), dim3(kRowX, kRowY), 0, s>>>(d_y, M, N, n, d_img);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -444,7 +485,7 @@ cudaError_t launch_fft_output_to_images(const float *d_y, int M, int N, int n, f
 cudaError_t launch_images_to_fft_input(const float *d_img, int N, int M, int n, float *d_x, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    images_to_fft_input_kernel<<<grid_for((size_t)M * M * n, kT), kT, 0, s>>>(d_img, N, M, n, d_x);
+    images_to_fft_input_kernel<<<row_grid(M, n), dim3(kRowX, kRowY), 0, s>>>(d_img, N, M, n, d_x);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -453,10 +494,14 @@ cudaError_t launch_spectrum_to_cas_images(const cufftComplex *d_spec, int M, int
                                           const float *d_scale, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    const unsigned g = grid_for((size_t)M * M * n, kT);
-    if (prec == kF32) spectrum_to_cas_images_kernel<float><<<g, kT, 0, s>>>(d_spec, M, n, (float *)d_cas, d_scale);
-    else if (prec == kF16) spectrum_to_cas_images_kernel<__half><<<g, kT, 0, s>>>(d_spec, M, n, (__half *)d_cas, d_scale);
-    else spectrum_to_cas_images_kernel<__nv_bfloat16><<<g, kT, 0, s>>>(d_spec, M, n, (__nv_bfloat16 *)d_cas, d_scale);
+    const dim3 g = row_grid(M, n), b(kRowX, kRowY);
+    if (prec == kF32)
+        spectrum_to_cas_images_kernel<float, false><<<g, b, 0, s>>>(d_spec, M, n, (float *)d_cas, d_scale, 1.0f);
+    else if (prec == kF16)
+        spectrum_to_cas_images_kernel<__half, false><<<g, b, 0, s>>>(d_spec, M, n, (__half *)d_cas, d_scale, 1.0f);
+    else
+        spectrum_to_cas_images_kernel<__nv_bfloat16, false><<<g, b, 0, s>>>(d_spec, M, n, (__nv_bfloat16 *)d_cas,
+                                                                             d_scale, 1.0f);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -464,7 +509,8 @@ cudaError_t launch_spectrum_to_cas_images(const cufftComplex *d_spec, int M, int
 cudaError_t launch_spectrum_to_cas_images_adjoint(const cufftComplex *d_spec, int M, int n, float *d_cas, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
-    spectrum_to_cas_images_adjoint_kernel<<<grid_for((size_t)M * M * n, kT), kT, 0, s>>>(d_spec, M, n, d_cas);
+    spectrum_to_cas_images_kernel<float, true><<<row_grid(M, n), dim3(kRowX, kRowY), 0, s>>>(
+        d_spec, M, n, d_cas, nullptr, 1.0f / ((float)M * (float)M));
     count_launches(1);
     return cudaGetLastError();
 }
@@ -568,7 +614,7 @@ cudaError_t launch_ctf(float *d_mul, int mul_power, float *d_gen, int gen_power,
     const double A = c.amp_contrast;
     k.w_sin = (float)std::sqrt(1.0 - A * A);
     k.w_cos = (float)A;
-    ctf_kernel<<<grid_for((size_t)M * M * n, kT), kT, 0, s>>>(d_mul, d_gen, M, n, d_defocus, k, mul_power, gen_power);
+    ctf_kernel<<<row_grid(M, n), dim3(kRowX, kRowY), 0, s>>>(d_mul, d_gen, M, n, d_defocus, k, mul_power, gen_power);
     count_launches(1);
     return cudaGetLastError();
 }
