@@ -136,13 +136,13 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(vol, axes, args):
+def cpu_baseline(vol, axes, args, threads=None, sample=None):
     from oracle import cpu_path, oracle as O
 
     p = O.Params(args.size)
-    S = min(args.cpu_sample, len(axes))
+    S = min(sample or args.cpu_sample, len(axes))
     idx = np.linspace(0, len(axes) - 1, S).round().astype(int)
-    t_step, det = cpu_path.time_step(vol, axes[idx], p, len(axes))
+    t_step, det = cpu_path.time_step(vol, axes[idx], p, len(axes), threads=threads)
     return len(axes) / t_step, det, S
 
 
@@ -294,6 +294,10 @@ def run_gb300(args):
         v, det, S = cpu_baseline(vol, axes, args)
         base = {"value": v, "unit": UNIT, "cores": det["threads"], "kind": "port",
                 "sample": "%d of %d directions timed, step extrapolated (t_fixed + D/S * t_sample)" % (S, n)}
+        # the same port on one core, on a smaller sample
+        v1, _, S1 = cpu_baseline(vol, axes, args, threads=1, sample=max(1, args.cpu_sample // 8))
+        base["one_core"] = {"value": v1, "cores": 1,
+                            "sample": "%d of %d directions timed on one thread, step extrapolated" % (S1, n)}
 
     g.close()
     serve = prec = grad = ctf = None

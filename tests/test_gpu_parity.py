@@ -240,6 +240,27 @@ def test_reconstruct_volume(cuda):
     assert O.rel_l2(rec, ref) < TOL
 
 
+def test_cpu_runnable_workload(cuda):
+    """The reference's CPU-runnable configuration at full size: 64^3, 20
+    Gaussian blobs (seed 1), 1,000 random-quaternion directions (seed 1),
+    interpFactor 2 (CAS images 128^2, CAS volume 134^3): forwardProject and
+    reconstructVol against the oracle's FP32 restatement."""
+    import multigpugridder_gb300 as gg
+
+    N = 64
+    p = O.Params(N)
+    vol = O.blob_volume(N, 20, seed=1)
+    axes = O.quaternion_axes(1000, seed=1).astype(np.float32)
+    with gg.MultiGPUGridder(N, len(axes), adjustInterpFactor=False) as g:
+        g.setVolume(vol)
+        imgs = g.forwardProject(axes)
+        rec = g.reconstructVol(imgs, axes)
+    ref_imgs, _ = O.forward_project(vol, axes, p, precision="f32")
+    assert O.rel_l2(imgs, ref_imgs) < TOL
+    ref_rec, _, _ = O.reconstruct_vol(imgs, axes, p, precision="f32")
+    assert O.rel_l2(rec, ref_rec) < TOL
+
+
 def test_fp_sphere_known_answer(cuda):
     """ForwardProjectTests.m:28-69: a fuzzy sphere projects to sum(V, 3) in
     every direction; max |mean(image - GT)| <= 1."""
