@@ -481,6 +481,68 @@ __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase
     }
 }
 
+// foot_window with adjacent pixels of a row taken in pairs by the packed
+// FP32x2 instructions (sm_100+): the pixel positions, the table indices and
+// the weight products of two pixels per instruction.  Each lane of a packed
+// instruction rounds as the scalar instruction does, so every weight, and
+// every sum (accumulated one pixel at a time in the same order), is
+// bit-identical to foot_window's.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+template <bool DENS, int WI, int WJ, int FS, bool DW = false>
+__device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fbase, unsigned tab, float pi0,
+                                               float pj0, float &cumSum, float &cumW, const float *fbase2 = nullptr)
+{
+    const float2 nx0 = f2(q.nx0, q.nx0), nx1 = f2(q.nx1, q.nx1), nx2 = f2(q.nx2, q.nx2);
+    const float2 vc = f2(q.vc, q.vc), sc = f2(q.s, q.s), mg = f2(12582912.0f, 12582912.0f);
+    const float2 c0 = f2(q.c0, q.c0), c1 = f2(q.c1, q.c1), c2 = f2(q.c2, q.c2);
+#pragma unroll
+    for (int jo = 0; jo < WJ; jo++) {
+        const float pj = pj0 + (float)jo;
+        const float py0 = __fmul_rn(pj, q.ny0), py1 = __fmul_rn(pj, q.ny1), py2 = __fmul_rn(pj, q.ny2);
+        const float2 qy0 = f2(py0, py0), qy1 = f2(py1, py1), qy2 = f2(py2, py2);
+#pragma unroll
+        for (int io = 0; io + 1 < WI; io += 2) {
+            const float2 pi = f2(pi0 + (float)io, pi0 + (float)(io + 1));
+            const float2 q0 = __fadd2_rn(__ffma2_rn(pi, nx0, qy0), vc);
+            const float2 q1 = __fadd2_rn(__ffma2_rn(pi, nx1, qy1), vc);
+            const float2 q2 = __fadd2_rn(__ffma2_rn(pi, nx2, qy2), vc);
+            const float2 b0 = __fadd2_rd(__ffma2_rn(q0, sc, c0), mg);
+            const float2 b1 = __fadd2_rd(__ffma2_rn(q1, sc, c1), mg);
+            const float2 b2 = __fadd2_rd(__ffma2_rn(q2, sc, c2), mg);
+            const float2 t0 = f2(lds_f32(tab + __float_as_uint(b0.x) * (4u * kTabRep)),
+                                 lds_f32(tab + __float_as_uint(b0.y) * (4u * kTabRep)));
+            const float2 t1 = f2(lds_f32(tab + __float_as_uint(b1.x) * (4u * kTabRep)),
+                                 lds_f32(tab + __float_as_uint(b1.y) * (4u * kTabRep)));
+            const float2 t2 = f2(lds_f32(tab + __float_as_uint(b2.x) * (4u * kTabRep)),
+                                 lds_f32(tab + __float_as_uint(b2.y) * (4u * kTabRep)));
+            const float2 w = __fmul2_rn(__fmul2_rn(t0, t1), t2);
+            cumSum = __fmaf_rn(fbase[jo * FS + io], w.x, cumSum);
+            if (DENS) cumW = __fadd_rn(cumW, w.x);
+            if (DW) cumW = __fmaf_rn(fbase2[jo * FS + io], w.x, cumW);
+            cumSum = __fmaf_rn(fbase[jo * FS + io + 1], w.y, cumSum);
+            if (DENS) cumW = __fadd_rn(cumW, w.y);
+            if (DW) cumW = __fmaf_rn(fbase2[jo * FS + io + 1], w.y, cumW);
+        }
+        if (WI & 1) {
+            constexpr int io = WI - 1;
+            const float pi = pi0 + (float)io;
+            const float q0 = __fadd_rn(__fmaf_rn(pi, q.nx0, py0), q.vc);
+            const float q1 = __fadd_rn(__fmaf_rn(pi, q.nx1, py1), q.vc);
+            const float q2 = __fadd_rn(__fmaf_rn(pi, q.nx2, py2), q.vc);
+            const unsigned b0 = __float_as_uint(__fadd_rd(__fmaf_rn(q0, q.s, q.c0), 12582912.0f));
+            const unsigned b1 = __float_as_uint(__fadd_rd(__fmaf_rn(q1, q.s, q.c1), 12582912.0f));
+            const unsigned b2 = __float_as_uint(__fadd_rd(__fmaf_rn(q2, q.s, q.c2), 12582912.0f));
+            float w = lds_f32(tab + b0 * (4u * kTabRep));
+            w = __fmul_rn(w, lds_f32(tab + b1 * (4u * kTabRep)));
+            w = __fmul_rn(w, lds_f32(tab + b2 * (4u * kTabRep)));
+            cumSum = __fmaf_rn(fbase[jo * FS + io], w, cumSum);
+            if (DENS) cumW = __fadd_rn(cumW, w);
+            if (DW) cumW = __fmaf_rn(fbase2[jo * FS + io], w, cumW);
+        }
+    }
+}
+
 // Table entries below and above the table a window can reach with
 // orthonormal axes: |Q - v| <= sqrt(2.5^2 + 2.5^2 + 2^2) < 4.1 per axis for
 // the reference window, sqrt(3.5^2 + 3.5^2 + 3.47^2) < 6.1 for the adjoint's.
@@ -752,7 +814,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                            kerCenterHalf - (float)vk * sg};
                         const float *fb = wfoot + rj * FS + ri;
                         const float pi0 = (float)(imgi - HALF - imgCenter), pj0 = (float)(imgj - HALF - imgCenter);
-                        foot_window<DENS, W, W, FS, DW>(fwin, fb, tab, pi0, pj0, cs, cw,
+                        foot_window_x2<DENS, W, W, FS, DW>(fwin, fb, tab, pi0, pj0, cs, cw,
                                                         DW ? wfoot2 + rj * FS + ri : nullptr);
                     } else if (ADJ) {
                         cs = adjoint_window_slow<TI>(vi, vj, vk, volCenter, nx0, nx1, nx2, ny0, ny1, ny2, img_ptr, M,
