@@ -144,8 +144,9 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
     __syncthreads();
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int lx = (lane & 7) | ((warp & 1) << 3);
-    const int ly = (lane >> 3) | ((warp >> 1) << 2);
+    // 8x4 warp tiles (2 x 4 per CTA), or with TR 4x8 tiles (4 x 2) when the
+    // copy's contiguous axis advances more per image row than per column, so
+    // that the eight-pixel side of a warp runs along the volume's rows
     const int ic = M / 2, vc = V / 2;
     const float kerCenter = ((float)kerSize - 1) / 2;
     const float kerScale = kerCenter / kerHW;
@@ -159,6 +160,18 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
     for (long long item = blockIdx.x; item < nItems; item += gridDim.x) {
         const int a = (int)(item / tilesPerImg);
         const int t = (int)(item - (long long)a * tilesPerImg);
+        const float *ax = axes + 9 * (size_t)a;
+        // the copy (layout 0: x, 1: y, 2: z contiguous) whose contiguous axis
+        // is the most perpendicular to the direction
+        int lay = 0;
+        bool tall = false;
+        if (TR) {
+            const float nz0 = fabsf(__ldg(ax + 6)), nz1 = fabsf(__ldg(ax + 7)), nz2 = fabsf(__ldg(ax + 8));
+            lay = (nz1 < nz0 && nz1 <= nz2) ? 1 : (nz2 < nz0 && nz2 < nz1) ? 2 : 0;
+            tall = fabsf(__ldg(ax + 3 + lay)) > fabsf(__ldg(ax + lay));
+        }
+        const int lx = tall ? (lane >> 3) | ((warp & 3) << 2) : (lane & 7) | ((warp & 1) << 3);
+        const int ly = tall ? (lane & 7) | ((warp >> 2) << 3) : (lane >> 3) | ((warp >> 1) << 2);
         const int i = (t % tilesX) * kFpTile + lx;
         const int j = (t / tilesX) * kFpTile + ly;
         if (i >= M || j >= M) continue;
@@ -168,7 +181,6 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
             *out = 0.0f;
             continue;
         }
-        const float *ax = axes + 9 * (size_t)a;
         const float nx0 = __ldg(ax + 0), nx1 = __ldg(ax + 1), nx2 = __ldg(ax + 2);
         const float ny0 = __ldg(ax + 3), ny1 = __ldg(ax + 4), ny2 = __ldg(ax + 5);
         const float fi = sample_coord(nx0, ny0, di, dj, vc);
@@ -203,12 +215,7 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
         float acc = 0.0f;
         const bool inside = b0 >= 0 && b1 >= 0 && b2 >= 0 && b0 + TAPS <= V && b1 + TAPS <= V && b2 + TAPS <= V;
         if (VEC && inside) {
-            // the copy (layout 0: x, 1: y, 2: z contiguous) and its axes, fastest first
-            int lay = 0;
-            if (TR) {
-                const float nz0 = fabsf(__ldg(ax + 6)), nz1 = fabsf(__ldg(ax + 7)), nz2 = fabsf(__ldg(ax + 8));
-                lay = (nz1 < nz0 && nz1 <= nz2) ? 1 : (nz2 < nz0 && nz2 < nz1) ? 2 : 0;
-            }
+            // the copy's axes, fastest first
             const int bc = lay == 0 ? b0 : lay == 1 ? b1 : b2;       // contiguous axis
             const int bb = lay == 0 ? b1 : b0;                        // middle axis
             const int ba = lay == 2 ? b1 : b2;                        // outer axis
@@ -238,8 +245,6 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
                 }
             }
         } else if (TR && inside) {
-            const float nz0 = fabsf(__ldg(ax + 6)), nz1 = fabsf(__ldg(ax + 7)), nz2 = fabsf(__ldg(ax + 8));
-            const int lay = (nz1 < nz0 && nz1 <= nz2) ? 1 : (nz2 < nz0 && nz2 < nz1) ? 2 : 0;
             // element strides of x, y, z in the chosen copy
             const size_t sx = lay == 0 ? 1 : (size_t)V;
             const size_t sy = lay == 0 ? (size_t)V : lay == 1 ? 1 : VV;
