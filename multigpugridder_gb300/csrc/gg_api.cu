@@ -138,6 +138,7 @@ struct gg_gridder {
     int run_fft_on_device = 1;
     int verbose = 0;
     int max_batch = 1024;
+    bool fused_fft = false;     // fft2_fused_ok(N, M): the 2-D FFT stages run as one kernel each
     int nstreams_fp = 2, nstreams_bp = 2;
     int prec = kF32;
     int bp_mode = GG_BP_REF;
@@ -370,7 +371,9 @@ void fp_batch(gg_gridder *h, const float *d_axes, int b, float *cas_out, float *
                                  dense ? (const void *)h->cas_y.p : (const void *)(h->cas_fp.p + fp_copy_floats(h)),
                                  dense ? (const void *)h->cas_z.p : (const void *)(h->cas_fp.p + 2 * fp_copy_floats(h))));
     ps.done();
-    if (img_out) {
+    if (img_out && h->fused_fft) {
+        GG_CK(launch_cas_to_images_fused(cas_out, h->M, h->N, b, img_out, s));
+    } else if (img_out) {
         GG_CK(launch_cas_images_to_spectrum(cas_out, h->M, b, S.spec.p, s));
         cufftHandle p = plan2d(h, CUFFT_C2R, b);
         GG_CKF(cufftSetStream(p, s));
@@ -400,6 +403,10 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
                 src = S.casimg_lp.p;
                 scale = h->img_scale();
             }
+        } else if (h->fused_fft && h->prec != kF16) {
+            void *dst = h->prec == kF32 ? (void *)S.casimg.p : (void *)S.casimg_lp.p;
+            GG_CK(launch_images_to_cas_fused(img, h->N, h->M, b, dst, h->prec, false, s));
+            src = dst;
         } else {
             GG_CK(launch_images_to_fft_input(img, h->N, h->M, b, S.real.p, s));
             cufftHandle p = plan2d(h, CUFFT_R2C, b);
@@ -443,11 +450,15 @@ void ctf_batch(gg_gridder *h, const float *d_axes, int b, const float *img, cons
                const CtfParams &c, int sl, cudaStream_t s)
 {
     auto &S = h->slot[sl];
-    GG_CK(launch_images_to_fft_input(img, h->N, h->M, b, S.real.p, s));
-    cufftHandle p = plan2d(h, CUFFT_R2C, b);
-    GG_CKF(cufftSetStream(p, s));
-    GG_CKF(cufftExecR2C(p, S.real.p, S.spec.p));
-    GG_CK(launch_spectrum_to_cas_images(S.spec.p, h->M, b, S.casimg.p, kF32, nullptr, s));
+    if (h->fused_fft) {
+        GG_CK(launch_images_to_cas_fused(img, h->N, h->M, b, S.casimg.p, kF32, false, s));
+    } else {
+        GG_CK(launch_images_to_fft_input(img, h->N, h->M, b, S.real.p, s));
+        cufftHandle p = plan2d(h, CUFFT_R2C, b);
+        GG_CKF(cufftSetStream(p, s));
+        GG_CKF(cufftExecR2C(p, S.real.p, S.spec.p));
+        GG_CK(launch_spectrum_to_cas_images(S.spec.p, h->M, b, S.casimg.p, kF32, nullptr, s));
+    }
     // CAS images *= CTF, and CTF^2 into S.real (free after the R2C), in one pass
     GG_CK(launch_ctf(S.casimg.p, 1, S.real.p, 2, h->M, b, d_defocus, c, s));
     if (h->prec == kF32 && h->bp_mode != GG_BP_ADJOINT) {
@@ -480,11 +491,15 @@ void forward_adjoint(gg_gridder *h, const float *d_axes, int n, const float *d_i
         const int b = std::min(B, n - a0);
         ensure_slot(h, 0, B, false);
         auto &S = h->slot[0];
-        GG_CK(launch_images_to_fft_input(d_img_grad + (size_t)a0 * NN, h->N, h->M, b, S.real.p, s));
-        cufftHandle p = plan2d(h, CUFFT_R2C, b);
-        GG_CKF(cufftSetStream(p, s));
-        GG_CKF(cufftExecR2C(p, S.real.p, S.spec.p));
-        GG_CK(launch_spectrum_to_cas_images_adjoint(S.spec.p, h->M, b, S.casimg.p, s));
+        if (h->fused_fft) {
+            GG_CK(launch_images_to_cas_fused(d_img_grad + (size_t)a0 * NN, h->N, h->M, b, S.casimg.p, kF32, true, s));
+        } else {
+            GG_CK(launch_images_to_fft_input(d_img_grad + (size_t)a0 * NN, h->N, h->M, b, S.real.p, s));
+            cufftHandle p = plan2d(h, CUFFT_R2C, b);
+            GG_CKF(cufftSetStream(p, s));
+            GG_CKF(cufftExecR2C(p, S.real.p, S.spec.p));
+            GG_CK(launch_spectrum_to_cas_images_adjoint(S.spec.p, h->M, b, S.casimg.p, s));
+        }
         ProfScope ps(h, s, GG_KERNEL_BACK);
         GG_CK(launch_back_project_adjoint(h->adj.p, S.casimg.p, kF32, h->ker.p, d_axes + (size_t)a0 * 9, b, h->geom(),
                                           nullptr, !h->five_taps, s));
@@ -644,6 +659,7 @@ void init_handle(gg_gridder *h)
     GG_CK(cudaMemcpy(h->scales.p, ones, sizeof(ones), cudaMemcpyHostToDevice));
     h->work.ensure(1);
     GG_CK(cudaMemset(h->work.p, 0, sizeof(unsigned int)));
+    h->fused_fft = fft2_fused_ok(h->N, h->M);
 }
 
 void destroy_handle(gg_gridder *h)
@@ -1351,7 +1367,7 @@ bool gg::gridder_view(gg_gridder *h, GridderView *out)
     std::lock_guard<std::mutex> lock(h->mu);
     const bool t = h->prec == kF32 && h->cas_fp_valid;
     *out = GridderView{h->device, h->N, h->M, h->V, h->geom(), h->cas.p, t ? h->cas_y.p : nullptr,
-                       t ? h->cas_z.p : nullptr, h->ker.p, h->five_taps};
+                       t ? h->cas_z.p : nullptr, h->ker.p, h->five_taps, h->fused_fft};
     return true;
 }
 

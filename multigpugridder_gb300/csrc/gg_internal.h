@@ -144,6 +144,20 @@ struct CtfConsts {
 cudaError_t launch_ctf(float *d_mul, int mul_power, float *d_gen, int gen_power, int M, int n, const float *d_defocus,
                        const CtfParams &c, cudaStream_t s);
 
+// ---- fused 2-D FFT stages (gg_fft2.cu) ----------------------------------------
+// True when N, M take the fused kernels: M in {64, 128, 256}, N <= M/2, N a
+// multiple of M/16, and the shared memory fits.
+bool fft2_fused_ok(int N, int M);
+// Images n*N*N -> CAS images n*M*M in storage `prec` (FP32 or BF16; FP16
+// needs the spectrum's scale first and is refused), in one launch: the pad,
+// shifts, forward 2-D FFT and Re+Im of the path above.  adjoint: the gradient
+// form of launch_spectrum_to_cas_images_adjoint (FP32 only).
+cudaError_t launch_images_to_cas_fused(const float *d_img, int N, int M, int n, void *d_cas, int prec, bool adjoint,
+                                       cudaStream_t s);
+// CAS images n*M*M (FP32) -> images n*N*N in one launch: FromCAS, shifts,
+// inverse 2-D FFT, crop and 1/M^2.
+cudaError_t launch_cas_to_images_fused(const float *d_cas, int M, int N, int n, float *d_img, cudaStream_t s);
+
 // Adds to the process-wide count of kernels launched by this library.
 void count_launches(long long n);
 
@@ -158,6 +172,7 @@ struct GridderView {
     const float *cas_y, *cas_z; // its copies with y / z contiguous (may be null)
     const float *ker; // KB table
     bool five_taps;
+    bool fused_fft;   // fft2_fused_ok(N, M)
 };
 
 } // namespace gg

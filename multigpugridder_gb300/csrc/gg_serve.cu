@@ -246,21 +246,30 @@ void enqueue(gg_server *S, Request &r)
     }
     for (int c0 = 0; c0 < r.n; c0 += B) {
         const int b = std::min(B, r.n - c0);
-        const cufftHandle p = lane_plan(L, r.op == GG_OP_FORWARD ? CUFFT_C2R : CUFFT_R2C, v.M, pow2ceil(b));
+        const cufftHandle p =
+            v.fused_fft ? 0 : lane_plan(L, r.op == GG_OP_FORWARD ? CUFFT_C2R : CUFFT_R2C, v.M, pow2ceil(b));
         if (r.op == GG_OP_FORWARD) {
             GS_CK(launch_forward_project(v.cas, kF32, v.V, d_cas, v.ker, d_axes + (size_t)c0 * 9, b, v.g, v.five_taps,
                                          nullptr, s, v.cas_y, v.cas_z));
-            GS_CK(launch_cas_images_to_spectrum(d_cas, v.M, b, d_spec, s));
-            GS_CKF(cufftExecC2R(p, d_spec, d_real));
-            GS_CK(launch_fft_output_to_images(d_real, v.M, v.N, b, d_img, s));
+            if (v.fused_fft) {
+                GS_CK(launch_cas_to_images_fused(d_cas, v.M, v.N, b, d_img, s));
+            } else {
+                GS_CK(launch_cas_images_to_spectrum(d_cas, v.M, b, d_spec, s));
+                GS_CKF(cufftExecC2R(p, d_spec, d_real));
+                GS_CK(launch_fft_output_to_images(d_real, v.M, v.N, b, d_img, s));
+            }
             GS_CK(cudaMemcpyAsync(r.out + (size_t)c0 * NN, d_img, (size_t)b * NN * sizeof(float),
                                   cudaMemcpyDeviceToHost, s));
         } else {
             GS_CK(cudaMemcpyAsync(d_img, r.in + (size_t)c0 * NN, (size_t)b * NN * sizeof(float),
                                   cudaMemcpyHostToDevice, s));
-            GS_CK(launch_images_to_fft_input(d_img, v.N, v.M, b, d_real, s));
-            GS_CKF(cufftExecR2C(p, d_real, d_spec));
-            GS_CK(launch_spectrum_to_cas_images(d_spec, v.M, b, d_cas, kF32, nullptr, s));
+            if (v.fused_fft) {
+                GS_CK(launch_images_to_cas_fused(d_img, v.N, v.M, b, d_cas, kF32, false, s));
+            } else {
+                GS_CK(launch_images_to_fft_input(d_img, v.N, v.M, b, d_real, s));
+                GS_CKF(cufftExecR2C(p, d_real, d_spec));
+                GS_CK(launch_spectrum_to_cas_images(d_spec, v.M, b, d_cas, kF32, nullptr, s));
+            }
             GS_CK(launch_back_project_ref(d_acc, d_cas, kF32, false, v.ker, d_axes + (size_t)c0 * 9, b, v.g, nullptr,
                                           s));
         }
