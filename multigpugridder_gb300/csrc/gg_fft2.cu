@@ -64,7 +64,8 @@ __device__ __forceinline__ float2 tw_at(const FftTwiddles &t, int m, bool inv)
 // Per-lane twiddles of warp_fft.
 template <int R>
 struct LaneTw {
-    float2 stage[5]; // W_(2h)^(lane & (h-1)) for h = 16, 8, 4, 2, 1
+    float2 stage[5]; // W_(2h)^(lane & (h-1)) for h = 16, 8, 4, 2, 1 on the upper lanes, 1 on the lower
+    float sign[5];   // -1 on the upper lanes (lane & h), +1 on the lower
     float2 step[R];  // W_M^(n1 * br5(lane))
     float2 reg[R / 2 > 0 ? R / 2 : 1]; // W_R^m, m < R/2 (uniform)
 };
@@ -76,7 +77,9 @@ __device__ __forceinline__ void lane_twiddles(LaneTw<R> &lt, const FftTwiddles &
 #pragma unroll
     for (int st = 0; st < 5; st++) {
         const int h = 16 >> st;
-        lt.stage[st] = tw_at(t, (lane & (h - 1)) * (128 / h), INV);
+        const bool upper = (lane & h) != 0;
+        lt.stage[st] = upper ? tw_at(t, (lane & (h - 1)) * (128 / h), INV) : make_float2(1.0f, 0.0f);
+        lt.sign[st] = upper ? -1.0f : 1.0f;
     }
     const int k2 = br5(lane);
 #pragma unroll
@@ -132,18 +135,19 @@ __device__ __forceinline__ void reg_fft(float2 (&x)[R], const float2 *wr)
 template <int R, bool INV>
 __device__ __forceinline__ void warp_fft(float2 (&x)[R], const LaneTw<R> &lt, int lane)
 {
+    // lower lane: x + other; upper lane: (other - x) * W.  Both as
+    // fma(sign, x, other) (rounds as the add or subtract) times the lane's
+    // twiddle, which is exactly 1 on the lower lanes.
 #pragma unroll
     for (int st = 0; st < 5; st++) {
         const int h = 16 >> st;
-        const bool upper = (lane & h) != 0;
         const float2 w = lt.stage[st];
+        const float sg = lt.sign[st];
 #pragma unroll
         for (int n1 = 0; n1 < R; n1++) {
             const float ox = __shfl_xor_sync(0xffffffffu, x[n1].x, h);
             const float oy = __shfl_xor_sync(0xffffffffu, x[n1].y, h);
-            const float2 s = make_float2(x[n1].x + ox, x[n1].y + oy);
-            const float2 d = cmul(make_float2(ox - x[n1].x, oy - x[n1].y), w);
-            x[n1] = upper ? d : s;
+            x[n1] = cmul(make_float2(fmaf(sg, x[n1].x, ox), fmaf(sg, x[n1].y, oy)), w);
         }
     }
 #pragma unroll
