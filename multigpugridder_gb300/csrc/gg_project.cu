@@ -410,17 +410,31 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
 // Back projection, reference window rule
 // ---------------------------------------------------------------------------
 // Only the voxels inside a direction's slab (|f_imgk| <= 2, a few percent of
-// the volume) run the 25-pixel window.  A CTA owns a 16x8x8 brick and each
-// warp an 8x4x4 block of it, 4 voxels per lane: block voxel l = lane + 32 s
-// (x = l & 7, y = (l >> 3) & 3, z = l >> 5).  Per direction a warp tests its
-// 128 voxels against the slab, lists the active ones in shared memory and
+// the volume) run the 25-pixel window.  A CTA owns a 16x8x(2 BD) brick and
+// each warp an 8x4xBD block of it, BD voxels per lane: block voxel
+// l = lane + 32 s (x = l & 7, y = (l >> 3) & 3, z = l >> 5).  Per direction a
+// warp tests its 32 BD voxels against the slab, lists the active ones in shared memory and
 // runs them 32 at a time, one per lane.  Every voxel still receives its
 // directions one by one in order and its window in the reference's order, so
 // the per-voxel sums are those of the reference kernel's loops, bit for bit.
-constexpr int kCBX = 16, kCBY = 8, kCBZ = 8; // brick: 2x2x2 warp blocks of 8x4x4
+constexpr int kCBX = 16, kCBY = 8; // brick: 2x2x2 warp blocks of 8x4xBD (BD = 8, or 4 for ADJ / DW)
 constexpr int kCThreads = 256;
 static_assert(kBpChunk == kCThreads, "the cull compaction gives one direction per thread");
-constexpr int kWarpVox = 128;                // voxels per warp block
+// Depth of a warp block: 4 voxels, or 8 (DEEP) for the reference rule on
+// CAS images of 512^2 and more.  Deeper blocks have more active voxels per
+// direction (fewer idle lanes in the last round of 32) and stage a footprint
+// for twice the voxels, which pays where the images are large (each staging
+// reads from L2 or DRAM); on 256^2 images the 4-deep kernel measured 20%
+// faster.  The adjoint keeps 4 (its 7x7 windows would outgrow the footprint),
+// and so does the two-stack form (its second footprint would pass the 48 KB
+// of static shared memory).
+template <bool ADJ, bool DW, bool DEEP>
+struct BpShape {
+    static constexpr int BD = (ADJ || DW || !DEEP) ? 4 : 8;
+    static constexpr int WV = 32 * BD;                         // voxels per warp block
+    static constexpr int BZ = 2 * BD;                          // brick depth
+    static constexpr int FW = ADJ ? 24 : (BD == 8 ? 20 : 16);  // footprint width and height
+};
 
 // The fast window.  For a voxel coordinate v and a window pixel whose
 // volume-frame position along the same axis is Q, the reference's table
@@ -439,8 +453,7 @@ constexpr int kWarpVox = 128;                // voxels per warp block
 // window of the warp's block can touch, staged per direction with the
 // reference's linear-index rule (a pixel whose index falls outside the image
 // reads as zero), so the windows read them at constant offsets.
-constexpr int kFootW = 16; // reference-rule footprint width (the adjoint's is 24)
-constexpr int kTabRep = 1;                           // interleaved table copies
+constexpr int kTabRep = 1; // interleaved table copies
 
 __device__ __forceinline__ float lds_f32(unsigned addr)
 {
@@ -603,7 +616,7 @@ __device__ float adjoint_window_slow(int vi, int vj, int vk, int volCenter, floa
 // DW (reference rule, FP32 images): pd accumulates the back projection of a
 // second image stack img2 (the same directions) in the same pass, with the
 // same weights and summation order as a separate back projection of img2.
-template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false>
+template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false, bool DEEP = false>
 __global__ void __launch_bounds__(kCThreads, 3)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
@@ -612,7 +625,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
 {
     static_assert(!DW || (!ONES && !DENS && !ADJ), "the second image stack is a reference-rule option");
     constexpr int W = ADJ ? 7 : 5, HALF = W / 2;
-    constexpr int FW = ADJ ? 24 : kFootW, FH = FW, FS = FW + 1;
+    using Shape = BpShape<ADJ, DW, DEEP>;
+    constexpr int BD = Shape::BD, kWarpVox = Shape::WV, kCBZ = Shape::BZ;
+    constexpr int FW = Shape::FW, FH = FW, FS = FW + 1;
     extern __shared__ float stab[]; // (kerSize + 2 tabPad) entries x kTabRep copies
     __shared__ float sax[kBpChunk * 9];
     __shared__ int slist[kBpChunk];
@@ -630,7 +645,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     const int x0 = (blockIdx.x % bricksX) * kCBX;
     const int y0 = ((blockIdx.x / bricksX) % bricksY) * kCBY;
     const int z0 = (blockIdx.x / (bricksX * bricksY)) * kCBZ;
-    const int bx = x0 + (warp & 1) * 8, by = y0 + ((warp >> 1) & 1) * 4, bz = z0 + (warp >> 2) * 4;
+    const int bx = x0 + (warp & 1) * 8, by = y0 + ((warp >> 1) & 1) * 4, bz = z0 + (warp >> 2) * BD;
     const int volCenter = (int)((float)V) / 2;
     const int imgCenter = (int)((float)M) / 2;
 
@@ -659,7 +674,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     const long long reach2 = ADJ ? (long long)(maskR + 4) * (maskR + 4) : R2;
     unsigned inmask = 0;
 #pragma unroll
-    for (int s = 0; s < 4; s++) {
+    for (int s = 0; s < BD; s++) {
         const int lz = bz + s;
         const long long d2 = (long long)(lx - volCenter) * (lx - volCenter) + (long long)(ly - volCenter) * (ly - volCenter) +
                              (long long)(lz - volCenter) * (lz - volCenter);
@@ -671,13 +686,13 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     const float kerScale = kerCenter / kerHW;
     const float kerCenterHalf = kerCenter + 0.5f;
     const float ax0 = (float)lx - volCenter, ay0 = (float)ly - volCenter;
-    const float wcx = bx + 3.5f - volCenter, wcy = by + 1.5f - volCenter, wcz = bz + 1.5f - volCenter;
+    const float wcx = bx + 3.5f - volCenter, wcy = by + 1.5f - volCenter, wcz = bz + 0.5f * (BD - 1) - volCenter;
     // slab half-thickness: kerHW for the reference rule; for the adjoint, any
     // voxel within the 4^3 window of a sample point (|r| < 2 per axis)
     const float slab = ADJ ? 2.0f * 1.7320508f + kCullEps : kerHW + kCullEps;
     const int MM = M * M;
     // Directions are staged through shared memory in chunks, culled against
-    // the brick (compacted in order), then against each warp's 8x4x4 block.
+    // the brick (compacted in order), then against each warp's 8x4xBD block.
     const float bcx = x0 + 0.5f * (kCBX - 1) - volCenter, bcy = y0 + 0.5f * (kCBY - 1) - volCenter,
                 bcz = z0 + 0.5f * (kCBZ - 1) - volCenter;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -733,9 +748,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             const float slabD = ADJ && (e & kBpChunk)
                                     ? fminf(slab, 2.0f * (fabsf(nz0) + fabsf(nz1) + fabsf(nz2)) + kCullEps)
                                     : slab;
-            {   // the warp's 8x4x4 block against the slab (uniform)
+            {   // the warp's 8x4xBD block against the slab (uniform)
                 const float d = wcx * nz0 + wcy * nz1 + wcz * nz2;
-                const float ext = 0.5f * (7.0f * fabsf(nz0) + 3.0f * fabsf(nz1) + 3.0f * fabsf(nz2));
+                const float ext = 0.5f * (7.0f * fabsf(nz0) + 3.0f * fabsf(nz1) + (float)(BD - 1) * fabsf(nz2));
                 if (fabsf(d) > slab + ext) continue;
             }
             // the reference's per-voxel slab test (gpuBackProject.cu:64-66), or
@@ -743,7 +758,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             // in lane order
             int total = 0;
 #pragma unroll
-            for (int s = 0; s < 4; s++) {
+            for (int s = 0; s < BD; s++) {
                 const float az = (float)(bz + s) - volCenter;
                 const float fk = voxel_proj(ax0, ay0, az, nz0, nz1, nz2);
                 const bool act = ((inmask >> s) & 1u) && (ADJ ? fabsf(fk) < slabD : fabsf(fk) <= kerHW);
@@ -763,8 +778,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             if (e & kBpChunk) {
                 const float ic = wcx * nx0 + wcy * nx1 + wcz * nx2 + (float)imgCenter;
                 const float jc = wcx * ny0 + wcy * ny1 + wcz * ny2 + (float)imgCenter;
-                const float hi = 3.5f * fabsf(nx0) + 1.5f * fabsf(nx1) + 1.5f * fabsf(nx2);
-                const float hj = 3.5f * fabsf(ny0) + 1.5f * fabsf(ny1) + 1.5f * fabsf(ny2);
+                const float hz = 0.5f * (float)(BD - 1);
+                const float hi = 3.5f * fabsf(nx0) + 1.5f * fabsf(nx1) + hz * fabsf(nx2);
+                const float hj = 3.5f * fabsf(ny0) + 1.5f * fabsf(ny1) + hz * fabsf(ny2);
                 fi0 = (int)floorf(ic - hi - 0.6f) - HALF;
                 fj0 = (int)floorf(jc - hj - 0.6f) - HALF;
                 const int fw = (int)floorf(ic + hi + 0.6f) + HALF - fi0 + 1;
@@ -772,8 +788,8 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 foot = fw <= FW && fh <= FH && fh >= W && (!ADJ || zeroEdges);
                 if (foot && !ADJ) {
                     // the reference's linear-index rule (gpuBackProject.cu:99)
-                    const int c = lane & (kFootW - 1);
-                    for (int r = lane >> 4; r < fh; r += 2) {
+                    for (int t = lane; t < fh * FW; t += 32) {
+                        const int r = t / FW, c = t - r * FW;
                         const int lin = (fj0 + r) * M + (fi0 + c);
                         float v = 0.0f, v2 = 0.0f;
                         if (lin >= 0 && lin < MM) {
@@ -845,7 +861,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     __syncwarp();
     const float sc = d_scale ? *d_scale : 1.0f;
 #pragma unroll
-    for (int s = 0; s < 4; s++) {
+    for (int s = 0; s < BD; s++) {
         if (!((inmask >> s) & 1u)) continue;
         const size_t o = (size_t)(bz + s) * V * V + (size_t)ly * V + lx;
         vol[o] = vol[o] + wacc[lane + 32 * s] * sc;
@@ -853,17 +869,18 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     }
 }
 
-template <typename TI, bool ONES, bool DENS = false, bool ADJ = false, bool DW = false>
+template <typename TI, bool ONES, bool DENS = false, bool ADJ = false, bool DW = false, bool DEEP = false>
 static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
                                        const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr,
                                        bool zero_edges = true, const float *img2 = nullptr)
 {
     if (n <= 0) return cudaSuccess;
+    constexpr int kCBZ = BpShape<ADJ, DW, DEEP>::BZ;
     const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
     const long long nb = (long long)bx * by * bz;
     const int pad = bp_table_pad(g.ker_size, ADJ);
     const size_t dyn = (size_t)(g.ker_size + 2 * pad) * kTabRep * sizeof(float);
-    auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW>;
+    auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
     kern<<<(unsigned)nb, kCThreads, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
@@ -872,23 +889,37 @@ static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *k
     return cudaGetLastError();
 }
 
+// Reference-rule launch with the block depth chosen by the image size.
+template <typename TI, bool ONES, bool DENS>
+static cudaError_t launch_bp_ref_sized(float *vol, const TI *img, const float *ker, const float *axes, int n,
+                                       const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr)
+{
+    if (g.M >= 512)
+        return launch_bp_compact_t<TI, ONES, DENS, false, false, true>(vol, img, ker, axes, n, g, scale, s, pd);
+    return launch_bp_compact_t<TI, ONES, DENS>(vol, img, ker, axes, n, g, scale, s, pd);
+}
+
 cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, bool ones, const float *d_ker,
                                     const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
 {
-    if (ones) return launch_bp_compact_t<float, true>(d_vol, nullptr, d_ker, d_axes, n, g, scale, s);
-    if (iprec == kF32) return launch_bp_compact_t<float, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
-    if (iprec == kF16) return launch_bp_compact_t<__half, false>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
-    return launch_bp_compact_t<__nv_bfloat16, false>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g, scale, s);
+    if (ones) return launch_bp_ref_sized<float, true, false>(d_vol, nullptr, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF32)
+        return launch_bp_ref_sized<float, false, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF16)
+        return launch_bp_ref_sized<__half, false, false>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
+    return launch_bp_ref_sized<__nv_bfloat16, false, false>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g,
+                                                            scale, s);
 }
 
 cudaError_t launch_back_project_ref_density(float *d_vol, float *d_pd, const void *d_img, int iprec, const float *d_ker,
                                             const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
 {
     if (iprec == kF32)
-        return launch_bp_compact_t<float, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
+        return launch_bp_ref_sized<float, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
     if (iprec == kF16)
-        return launch_bp_compact_t<__half, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
-    return launch_bp_compact_t<__nv_bfloat16, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g,
+        return launch_bp_ref_sized<__half, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s,
+                                                        d_pd);
+    return launch_bp_ref_sized<__nv_bfloat16, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g,
                                                            scale, s, d_pd);
 }
 
