@@ -420,17 +420,19 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
 constexpr int kCBX = 16, kCBY = 8; // brick: 2x2x2 warp blocks of 8x4xBD (BD = 8, or 4 for ADJ / DW)
 constexpr int kCThreads = 256;
 static_assert(kBpChunk == kCThreads, "the cull compaction gives one direction per thread");
-// Depth of a warp block: 4 voxels, or 8 (DEEP) for the reference rule on
-// CAS images of 512^2 and more.  Deeper blocks have more active voxels per
+// Depth of a warp block for the reference rule: 6 voxels, or 8 (DEEP) on CAS
+// images of 512^2 and more.  Deeper blocks have more active voxels per
 // direction (fewer idle lanes in the last round of 32) and stage a footprint
-// for twice the voxels, which pays where the images are large (each staging
-// reads from L2 or DRAM); on 256^2 images the 4-deep kernel measured 20%
-// faster.  The adjoint keeps 4 (its 7x7 windows would outgrow the footprint),
-// and so does the two-stack form (its second footprint would pass the 48 KB
-// of static shared memory).
+// for more voxels, which pays most where the images are large (each staging
+// reads from L2 or DRAM); on 256^2 images 8-deep blocks measured 20% slower
+// than 4-deep ones and 6-deep ones 0.7% faster.  With 6 the footprint still
+// fits 16 pixels for any orthonormal axes (2 |(3.5, 1.5, 2.5)| + 1.2 < 11).
+// The adjoint keeps 4 (its 7x7 windows would outgrow the footprint), and so
+// does the two-stack form (its second footprint would pass the 48 KB of
+// static shared memory).
 template <bool ADJ, bool DW, bool DEEP>
 struct BpShape {
-    static constexpr int BD = (ADJ || DW || !DEEP) ? 4 : 8;
+    static constexpr int BD = (ADJ || DW) ? 4 : (DEEP ? 8 : 6);
     static constexpr int WV = 32 * BD;                         // voxels per warp block
     static constexpr int BZ = 2 * BD;                          // brick depth
     static constexpr int FW = ADJ ? 24 : (BD == 8 ? 20 : 16);  // footprint width and height
