@@ -428,8 +428,8 @@ static_assert(kBpChunk == kCThreads, "the cull compaction gives one direction pe
 // than 4-deep ones and 6-deep ones 0.7% faster.  With 6 the footprint still
 // fits 16 pixels for any orthonormal axes (2 |(3.5, 1.5, 2.5)| + 1.2 < 11).
 // The adjoint keeps 4 (6-deep blocks fit its 24-wide footprint but measured
-// 4% slower on the gradient step), and so does the two-stack form (its
-// second footprint would pass the 48 KB of static shared memory).
+// 4% slower on the gradient step), and so does the two-stack form (6-deep
+// fits its 48 KB of static shared memory but measured no faster).
 template <bool ADJ, bool DW, bool DEEP>
 struct BpShape {
     static constexpr int BD = (ADJ || DW) ? 4 : (DEEP ? 8 : 6);
