@@ -162,6 +162,18 @@ __device__ __forceinline__ int wrap_src(int q, int N, int M)
     return q < N / 2 ? q + N / 2 : (q >= M - N / 2 ? q - (M - N / 2) : -1);
 }
 
+// Asynchronous 4-byte global -> shared copies (cp.async), to stage the next
+// image while the current one is transformed.
+__device__ __forceinline__ void cp_async4(float *dst, const float *src)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // Row r of an N-row block stored at row (r mod R) * (N / R) + r / R: the rows
 // R apart that one gather of a warp touches land in consecutive rows.
 template <int R>
@@ -187,14 +199,20 @@ fft_images_to_cas_kernel(const float *__restrict__ img, int N, int n, T *__restr
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     LaneTw<R> lt;
     lane_twiddles<R, false>(lt, tw, lane);
-
-    for (int a = blockIdx.x; a < n; a += gridDim.x) {
+    // image a -> simg (rows spread), asynchronously
+    auto stage = [&](int a) {
         const float *im = img + (size_t)a * N * N;
         for (int r = warp; r < N; r += nw) {
             float *dst = simg + spread<R>(r, N) * NP;
-            for (int c = lane; c < N; c += 32) dst[c] = __ldg(im + (size_t)r * N + c);
+            for (int c = lane; c < N; c += 32) cp_async4(dst + c, im + (size_t)r * N + c);
         }
-        __syncthreads();
+        cp_async_commit();
+    };
+    if ((int)blockIdx.x < n) stage(blockIdx.x);
+
+    for (int a = blockIdx.x; a < n; a += gridDim.x) {
+        cp_async_wait_all();
+        __syncthreads(); // image a is in simg
 
         // columns k and k + H of the image, along y
         for (int k = warp; k < H; k += nw) {
@@ -218,6 +236,8 @@ fft_images_to_cas_kernel(const float *__restrict__ img, int N, int n, T *__restr
             }
         }
         __syncthreads();
+        // simg is free: the next image loads while the rows are transformed
+        if (a + (int)gridDim.x < n) stage(a + gridDim.x);
 
         // rows v = 0 .. M/2, along x
         for (int v = warp; v <= M / 2; v += nw) {
@@ -259,6 +279,15 @@ fft_images_to_cas_kernel(const float *__restrict__ img, int N, int n, T *__restr
 }
 
 // ---- CAS images -> images ----------------------------------------------------
+// A staged CAS row (M floats) holds column c at (c mod R) * (M/R + 32/R) +
+// c / R: lanes that read columns R apart, or write consecutive ones, hit
+// distinct banks.  A staged row takes M + 32 floats.
+template <int R>
+__device__ __forceinline__ int row_slot(int c, int M)
+{
+    return (c % R) * (M / R + 32 / R) + c / R;
+}
+
 template <int M>
 __global__ void __launch_bounds__(kFftThreads, 1)
 fft_cas_to_images_kernel(const float *__restrict__ cas, int N, int n, float *__restrict__ img, const FftTwiddles tw)
@@ -269,7 +298,8 @@ fft_cas_to_images_kernel(const float *__restrict__ cas, int N, int n, float *__r
     const int H = N / 2, GP = N + 1, OP = N + 1;
     float *gre = sm;                 // g(p, v), v <= M/2 (spread), N output columns of GP
     float *gim = gre + R * GR * GP;
-    float *sout = gim + R * GR * GP; // N x OP output image
+    float *sout = gim + R * GR * GP; // N x OP output image; during the row pass, the warps'
+                                     // staged CAS rows (2 buffers x 2 rows x (M + 32), row_slot)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const float scale = 1.0f / ((float)M * (float)M);
     LaneTw<R> lt;
@@ -277,10 +307,34 @@ fft_cas_to_images_kernel(const float *__restrict__ cas, int N, int n, float *__r
 
     for (int a = blockIdx.x; a < n; a += gridDim.x) {
         const float *ca = cas + (size_t)a * M * M;
-        // rows v = 0 .. M/2 of the spectrum, along u, keeping the cropped p
-        for (int v = warp; v <= M / 2; v += nw) {
+        // rows v = 0 .. M/2 of the spectrum, along u, keeping the cropped p.
+        // Each warp stages CAS rows shift(v) and M - shift(v) of its next v
+        // while it transforms the current one.
+        constexpr int RL = M + 32; // staged row length
+        float *stg = sout + warp * (4 * RL);
+        auto fetch = [&](int v, int buf) {
             const int j = (v + M / 2) & (M - 1), jm = (M - j) & (M - 1);
             const float *rj = ca + (size_t)j * M, *rjm = ca + (size_t)jm * M;
+            float *b = stg + buf * (2 * RL);
+            for (int c = lane; c < M; c += 32) {
+                const int sc = row_slot<R>(c, M);
+                cp_async4(b + sc, rj + c);
+                cp_async4(b + RL + sc, rjm + c);
+            }
+            cp_async_commit();
+        };
+        fetch(warp, 0);
+        for (int v = warp, it = 0; v <= M / 2; v += nw, it++) {
+            const bool more = v + nw <= M / 2;
+            if (more) {
+                fetch(v + nw, (it + 1) & 1);
+                cp_async_wait_group<1>();
+            } else {
+                cp_async_wait_group<0>();
+            }
+            __syncwarp(); // row v is staged
+            const int j = (v + M / 2) & (M - 1);
+            const float *b = stg + (it & 1) * (2 * RL);
             float2 x[R];
 #pragma unroll
             for (int n1 = 0; n1 < R; n1++) {
@@ -288,10 +342,11 @@ fft_cas_to_images_kernel(const float *__restrict__ cas, int N, int n, float *__r
                 const int i = (u + M / 2) & (M - 1), im = (M - i) & (M - 1);
                 x[n1] = make_float2(0.f, 0.f);
                 if (i != 0 && j != 0) {
-                    const float c1 = __ldg(rj + i), c2 = __ldg(rjm + im);
+                    const float c1 = b[row_slot<R>(i, M)], c2 = b[RL + row_slot<R>(im, M)];
                     x[n1] = make_float2(0.5f * (c1 + c2), 0.5f * (c1 - c2));
                 }
             }
+            __syncwarp(); // the buffer may be refilled two rows later
             warp_fft<R, true>(x, lt, lane);
             const int gs = (v % R) * GR + v / R;
 #pragma unroll
@@ -378,7 +433,8 @@ static size_t fwd_smem(int N, int M) { return ((size_t)N * (N + 1) + 2 * (size_t
 static size_t inv_smem(int N, int M)
 {
     const int R = M / 32, GR = (M / 2) / R + 1;
-    return (2 * (size_t)R * GR * (N + 1) + (size_t)N * (N + 1)) * sizeof(float);
+    const size_t out = (size_t)N * (N + 1), stage = (size_t)(kFftThreads / 32) * 4 * (M + 32);
+    return (2 * (size_t)R * GR * (N + 1) + (out > stage ? out : stage)) * sizeof(float);
 }
 
 bool fft2_fused_ok(int N, int M)
