@@ -22,6 +22,9 @@
 //     the N output columns of the crop; then pairs of output columns are
 //     inverse-transformed along y (the missing rows v > M/2 are conjugates),
 //     keeping the N output rows, scaled by 1/M^2.
+// Inputs are staged with cp.async: the next image while the rows of the
+// current one are transformed, and each warp's next two CAS rows while it
+// transforms the current spectrum row.
 //
 // Each M-point FFT runs on one warp: M = R * 32, lane l holding elements
 // R*l .. R*l+R-1.  A 32-point decimation-in-frequency FFT across the lanes
