@@ -237,6 +237,9 @@ def run_gb300(args):
             ev[k][1].record(stream)
             flush.fill_(float(k))  # untimed L2 flush between steps
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
     launches = L.gg_kernel_launch_count() - launches0
     ms_steps = [a.elapsed_time(b) for a, b in ev]
     prof = {}
