@@ -157,8 +157,9 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
     const size_t VV = (size_t)V * V, PV = (size_t)P * V;
     const long long V3 = (long long)VV * V;
 
+    const bool items32 = nItems <= 0x7fffffffLL; // 32-bit division per item whenever it fits
     for (long long item = blockIdx.x; item < nItems; item += gridDim.x) {
-        const int a = (int)(item / tilesPerImg);
+        const int a = items32 ? (int)((unsigned)item / (unsigned)tilesPerImg) : (int)(item / tilesPerImg);
         const int t = (int)(item - (long long)a * tilesPerImg);
         const float *ax = axes + 9 * (size_t)a;
         // the copy (layout 0: x, 1: y, 2: z contiguous) whose contiguous axis
