@@ -407,6 +407,14 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
             void *dst = h->prec == kF32 ? (void *)S.casimg.p : (void *)S.casimg_lp.p;
             GG_CK(launch_images_to_cas_fused(img, h->N, h->M, b, dst, h->prec, false, s));
             src = dst;
+        } else if (h->fused_fft) {
+            // FP16: FP32 CAS images first, then the storage scale from their
+            // largest magnitude and the conversion
+            GG_CK(launch_images_to_cas_fused(img, h->N, h->M, b, S.casimg.p, kF32, false, s));
+            GG_CK(launch_storage_scale(S.casimg.p, MM * b, 8192.0f, h->work.p, h->scales.p + 1, s));
+            GG_CK(launch_convert(S.casimg.p, S.casimg_lp.p, h->prec, MM * b, h->img_scale(), s));
+            src = S.casimg_lp.p;
+            scale = h->img_scale();
         } else {
             GG_CK(launch_images_to_fft_input(img, h->N, h->M, b, S.real.p, s));
             cufftHandle p = plan2d(h, CUFFT_R2C, b);
