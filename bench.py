@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--cpu-sample", type=int, default=64)
+    ap.add_argument("--cpu-sample", type=int, default=1024,
+                    help="directions timed by the CPU baseline / reference arm per step (one core: 1/8 of it)")
     ap.add_argument("--serve-seconds", type=float, default=2.0,
                     help="arrival window of the serving workload (0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (Poisson)")
