@@ -1,9 +1,9 @@
 /*
  * CPU oracle for the Kaiser-Bessel Fourier-slice projection path.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker: only tests/, the smoke
- * check in __graft_entry__.py and the cpu_baseline / reference arm of bench.py
- * load it. The product (libgg_gridder.so) never links or calls it.
+ * TEST INFRASTRUCTURE ONLY. Only tests/, the smoke check in __graft_entry__.py
+ * and the CPU-baseline / reference arm of bench.py load it. The product
+ * (libgg_gridder.so) never links or calls it.
  *
  * It restates, loop for loop, the two projection kernels of
  * tagarelab/MultiGPUGridder:
