@@ -612,8 +612,8 @@ def run_ctf(args, vol, axes):
     check(L.gg_set_volume_dev(h, vp(d_vol), sp), h)
     check(L.gg_forward_project_dev(h, vp(d_ax), n, vp(d_img), None, sp), h)
     calls = {"plain": lambda: check(L.gg_reconstruct_volume_dev(h, vp(d_ax), n, vp(d_img), vp(d_out), sp), h),
-             "ctf": lambda: check(L.gg_reconstruct_volume_ctf_dev(h, vp(d_ax), n, vp(d_img), vp(df), 300.0, 2.7, 0.1,
-                                                                  1.0, vp(d_out), sp), h)}
+             "ctf": lambda: check(L.gg_reconstruct_volume_ctf_dev(h, vp(d_ax), n, vp(d_img), vp(df), None, None, 300.0,
+                                                                  2.7, 0.1, 1.0, vp(d_out), sp), h)}
     res = {}
     for name, call in calls.items():
         for _ in range(max(3, args.warmup)):

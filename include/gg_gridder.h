@@ -148,15 +148,19 @@ int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int n_axes,
    chi = pi lambda df s^2 - (pi/2) Cs lambda^3 s^4, s the spatial frequency
    (1/Å) of the padded image's pixel, lambda the relativistic electron
    wavelength at voltage_kv.  defocus: n_axes values in Å (underfocus
-   positive); cs_mm in mm; amp_contrast A in [0, 1]; pixel_size: Å per pixel
-   of the N x N images.  With defocus 0, Cs 0 and A = 1 the CTF is -1 and the
-   result equals gg_reconstruct_volume's. */
+   positive).  Astigmatism (both NULL for none): defocus_v, n_axes defoci V
+   in Å (defocus is then U), and astig_angle, n_axes angles in radians of the
+   U axis from the image x axis; df at frequency angle theta is
+   (U + V)/2 + (U - V)/2 cos 2(theta - angle).  cs_mm in mm; amp_contrast A
+   in [0, 1]; pixel_size: Å per pixel of the N x N images.  With defocus 0,
+   Cs 0 and A = 1 the CTF is -1 and the result equals gg_reconstruct_volume's. */
 int gg_reconstruct_volume_ctf(gg_gridder *h, const float *axes, int n_axes, const float *images,
-                              const float *defocus, float voltage_kv, float cs_mm, float amp_contrast,
-                              float pixel_size, float *volume_out);
+                              const float *defocus, const float *defocus_v, const float *astig_angle,
+                              float voltage_kv, float cs_mm, float amp_contrast, float pixel_size, float *volume_out);
 int gg_reconstruct_volume_ctf_dev(gg_gridder *h, const float *d_axes, int n_axes, const float *d_images,
-                                  const float *d_defocus, float voltage_kv, float cs_mm, float amp_contrast,
-                                  float pixel_size, float *d_volume_out, void *stream);
+                                  const float *d_defocus, const float *d_defocus_v, const float *d_astig_angle,
+                                  float voltage_kv, float cs_mm, float amp_contrast, float pixel_size,
+                                  float *d_volume_out, void *stream);
 
 /* Exact adjoint of the whole forward operator (setVolume's CAS preparation
    followed by forwardProject to images): image gradients n*N*N -> volume
@@ -234,9 +238,11 @@ int gg_filter_complex_to_real(const float *d_complex, float *d_real, int size, i
 /* CTF on CAS images (n_images * size^2, the gridder's CAS-image layout, DC at
    (size/2, size/2)): generate = 0 multiplies them by CTF^power, generate = 1
    overwrites them with CTF^power (power 1 or 2).  Parameters as for
-   gg_reconstruct_volume_ctf.  No counterpart in the reference. */
-int gg_filter_apply_ctf(float *d_cas_images, int size, int n_images, const float *d_defocus, float voltage_kv,
-                        float cs_mm, float amp_contrast, float pixel_size, int power, int generate, void *stream);
+   gg_reconstruct_volume_ctf (d_defocus_v and d_astig_angle both NULL for no
+   astigmatism).  No counterpart in the reference. */
+int gg_filter_apply_ctf(float *d_cas_images, int size, int n_images, const float *d_defocus,
+                        const float *d_defocus_v, const float *d_astig_angle, float voltage_kv, float cs_mm,
+                        float amp_contrast, float pixel_size, int power, int generate, void *stream);
 
 /* Host helpers: the KB lookup table (getKernelFiltTable.m:1-22) and the
    pre-compensation vector (getPreComp.m:1-28), computed in FP64. */

@@ -70,9 +70,10 @@ SIGNATURES = {
     "gg_back_project_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _c_int, _vp]),
     "gg_get_volume_dev": (_c_int, [_vp, _fp, _vp]),
     "gg_reconstruct_volume_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _vp]),
-    "gg_reconstruct_volume_ctf": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _c_float, _c_float, _c_float, _c_float, _fp]),
-    "gg_reconstruct_volume_ctf_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _c_float, _c_float, _c_float, _c_float,
-                                               _fp, _vp]),
+    "gg_reconstruct_volume_ctf": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _fp, _fp, _c_float, _c_float, _c_float,
+                                           _c_float, _fp]),
+    "gg_reconstruct_volume_ctf_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _fp, _fp, _c_float, _c_float, _c_float,
+                                               _c_float, _fp, _vp]),
     "gg_forward_project_adjoint": (_c_int, [_vp, _fp, _c_int, _fp, _fp]),
     "gg_forward_project_adjoint_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _vp]),
     "gg_forward_project_kernel": (_c_int, [_fp, _fp, _fp, _fp, _c_float, _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _vp]),
@@ -92,8 +93,8 @@ SIGNATURES = {
     "gg_filter_divide_scalar": (_c_int, [_fp, _c_float, _c_int, _c_int, _vp]),
     "gg_filter_real_to_complex": (_c_int, [_fp, _fp, _c_int, _c_int, _vp]),
     "gg_filter_complex_to_real": (_c_int, [_fp, _fp, _c_int, _c_int, _vp]),
-    "gg_filter_apply_ctf": (_c_int, [_fp, _c_int, _c_int, _fp, _c_float, _c_float, _c_float, _c_float, _c_int, _c_int,
-                                     _vp]),
+    "gg_filter_apply_ctf": (_c_int, [_fp, _c_int, _c_int, _fp, _fp, _fp, _c_float, _c_float, _c_float, _c_float, _c_int,
+                                     _c_int, _vp]),
     "gg_kb_table": (_c_int, [_c_int, _c_int, _dp]),
     "gg_precomp": (_c_int, [_c_int, _c_int, _dp]),
     "gg_kernel_launch_count": (ctypes.c_longlong, []),

@@ -455,7 +455,7 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
 // the CTF are back-projected into h->cas, and CTF^2 images into h->pd (the
 // CTF-weighted plane density), both by the gridder's back-projection rule.
 void ctf_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const float *d_defocus,
-               const CtfParams &c, int sl, cudaStream_t s)
+               const float *d_defocus_v, const float *d_astig, const CtfParams &c, int sl, cudaStream_t s)
 {
     auto &S = h->slot[sl];
     if (h->fused_fft) {
@@ -468,7 +468,7 @@ void ctf_batch(gg_gridder *h, const float *d_axes, int b, const float *img, cons
         GG_CK(launch_spectrum_to_cas_images(S.spec.p, h->M, b, S.casimg.p, kF32, nullptr, s));
     }
     // CAS images *= CTF, and CTF^2 into S.real (free after the R2C), in one pass
-    GG_CK(launch_ctf(S.casimg.p, 1, S.real.p, 2, h->M, b, d_defocus, c, s));
+    GG_CK(launch_ctf(S.casimg.p, 1, S.real.p, 2, h->M, b, d_defocus, d_defocus_v, d_astig, c, s));
     if (h->prec == kF32 && h->bp_mode != GG_BP_ADJOINT) {
         // both stacks in one back-projection pass
         ProfScope ps(h, s, GG_KERNEL_BACK);
@@ -1152,13 +1152,16 @@ extern "C" int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int
 }
 
 extern "C" int gg_reconstruct_volume_ctf_dev(gg_gridder *h, const float *d_axes, int n_axes, const float *d_images,
-                                             const float *d_defocus, float voltage_kv, float cs_mm, float amp_contrast,
-                                             float pixel_size, float *d_volume_out, void *stream)
+                                             const float *d_defocus, const float *d_defocus_v,
+                                             const float *d_astig_angle, float voltage_kv, float cs_mm,
+                                             float amp_contrast, float pixel_size, float *d_volume_out, void *stream)
 {
     return guarded(h, [&] {
         check_axes_count(n_axes);
         if (n_axes > 0 && (!d_axes || !d_images || !d_defocus))
             fail(GG_ERR_INVALID_ARG, "axes, images and defocus are required");
+        if ((d_defocus_v == nullptr) != (d_astig_angle == nullptr))
+            fail(GG_ERR_INVALID_ARG, "defocus_v and astig_angle are given together or not at all");
         if (!d_volume_out) fail(GG_ERR_INVALID_ARG, "output is NULL");
         const CtfParams c{voltage_kv, cs_mm, amp_contrast, pixel_size};
         check_ctf(c);
@@ -1173,7 +1176,9 @@ extern "C" int gg_reconstruct_volume_ctf_dev(gg_gridder *h, const float *d_axes,
         for (int a0 = 0; a0 < n_axes; a0 += B) {
             const int b = std::min(B, n_axes - a0);
             ensure_slot(h, 0, B, false);
-            ctf_batch(h, d_axes + (size_t)a0 * 9, b, d_images + (size_t)a0 * NN, d_defocus + a0, c, 0, s);
+            ctf_batch(h, d_axes + (size_t)a0 * 9, b, d_images + (size_t)a0 * NN, d_defocus + a0,
+                      d_defocus_v ? d_defocus_v + a0 : nullptr, d_astig_angle ? d_astig_angle + a0 : nullptr, c, 0,
+                      s);
         }
         GG_CK(launch_divide_plane_density(h->cas.p, h->pd.p, V3, 1e-6f, s));
         do_get_volume(h, h->cas.p, d_volume_out, s);
@@ -1183,29 +1188,43 @@ extern "C" int gg_reconstruct_volume_ctf_dev(gg_gridder *h, const float *d_axes,
 }
 
 extern "C" int gg_reconstruct_volume_ctf(gg_gridder *h, const float *axes, int n_axes, const float *images,
-                                         const float *defocus, float voltage_kv, float cs_mm, float amp_contrast,
-                                         float pixel_size, float *volume_out)
+                                         const float *defocus, const float *defocus_v, const float *astig_angle,
+                                         float voltage_kv, float cs_mm, float amp_contrast, float pixel_size,
+                                         float *volume_out)
 {
     return guarded(h, [&] {
         check_axes_count(n_axes);
         if (n_axes > 0 && (!axes || !images || !defocus))
             fail(GG_ERR_INVALID_ARG, "axes, images and defocus are required");
+        if ((defocus_v == nullptr) != (astig_angle == nullptr))
+            fail(GG_ERR_INVALID_ARG, "defocus_v and astig_angle are given together or not at all");
         if (!volume_out) fail(GG_ERR_INVALID_ARG, "output is NULL");
         const CtfParams c{voltage_kv, cs_mm, amp_contrast, pixel_size};
         check_ctf(c);
         cudaStream_t s = h->cs;
         const size_t V3 = (size_t)h->V * h->V * h->V, NN = (size_t)h->N * h->N, N3 = NN * h->N;
         upload_axes(h, axes, n_axes, s);
+        // per-image CTF parameters: defocus U, then (astigmatic) defocus V and angle
+        const bool astig = defocus_v != nullptr;
+        const size_t nn = (size_t)std::max(1, n_axes);
         DevBuf<float> df;
-        df.ensure((size_t)std::max(1, n_axes));
-        if (n_axes > 0) GG_CK(cudaMemcpyAsync(df.p, defocus, (size_t)n_axes * sizeof(float), cudaMemcpyHostToDevice, s));
+        df.ensure(astig ? 3 * nn : nn);
+        if (n_axes > 0) {
+            GG_CK(cudaMemcpyAsync(df.p, defocus, (size_t)n_axes * sizeof(float), cudaMemcpyHostToDevice, s));
+            if (astig) {
+                GG_CK(cudaMemcpyAsync(df.p + nn, defocus_v, (size_t)n_axes * sizeof(float), cudaMemcpyHostToDevice, s));
+                GG_CK(cudaMemcpyAsync(df.p + 2 * nn, astig_angle, (size_t)n_axes * sizeof(float),
+                                      cudaMemcpyHostToDevice, s));
+            }
+        }
         h->cas.ensure(V3);
         h->pd.ensure(V3);
         GG_CK(cudaMemsetAsync(h->cas.p, 0, V3 * sizeof(float), s));
         GG_CK(cudaMemsetAsync(h->pd.p, 0, V3 * sizeof(float), s));
         if (n_axes > 0)
             host_batches(h, n_axes, images, NN, false, [&](int a0, int b, int sl, float *dbuf) {
-                ctf_batch(h, h->axes.p + (size_t)a0 * 9, b, dbuf, df.p + a0, c, sl, s);
+                ctf_batch(h, h->axes.p + (size_t)a0 * 9, b, dbuf, df.p + a0, astig ? df.p + nn + a0 : nullptr,
+                          astig ? df.p + 2 * nn + a0 : nullptr, c, sl, s);
             });
         GG_CK(launch_divide_plane_density(h->cas.p, h->pd.p, V3, 1e-6f, s));
         h->vol_io.ensure(N3);

@@ -367,27 +367,68 @@ __global__ void transpose_volume_kernel(const float *__restrict__ in, int V, flo
 // first two short enough that k * part is exact); sincosf then sees |r| <= pi.
 // A real, even CTF multiplies Re and Im alike, so it applies to CAS images
 // directly.  d_mul (optional) *= CTF^mul_power; d_gen (optional) = CTF^gen_power.
+// ASTIG: per-image astigmatism, defocus_v and astig (radians, from the x
+// axis) given.  The defocus at angle theta is df_m + df_d cos 2(theta - phi)
+// with df_m, df_d the mean and half-difference of defocus U and V; with
+// (dx, dy) the pixel's offset from DC, alpha df s^2 becomes
+// alpha (df_m r2 + df_d ((dx^2 - dy^2) cos 2phi + 2 dx dy sin 2phi)), no
+// division.  alpha df_m, alpha df_d, cos 2phi and sin 2phi are formed in FP64
+// once per image and row and split into float pairs; the per-pixel terms
+// stay float-float as above.
+template <bool ASTIG>
 __global__ void __launch_bounds__(kRowX *kRowY)
 ctf_kernel(float *__restrict__ d_mul, float *__restrict__ d_gen, int M, int n, const float *__restrict__ defocus,
-           CtfConsts k, int mul_power, int gen_power)
+           const float *__restrict__ defocus_v, const float *__restrict__ astig, CtfConsts k, int mul_power,
+           int gen_power)
 {
     const int j = blockIdx.x * kRowY + threadIdx.y;
     if (j >= M) return;
     const int dj = j - M / 2;
     for (int a = blockIdx.y; a < n; a += gridDim.y) {
-        const float df = defocus[a];
-        // c = alpha * df as hi + lo (the rounded products are __fmul_rn so
-        // that no FMA contraction changes them: the error terms below assume
-        // each one rounded on its own)
-        const float c_hi = __fmul_rn(k.a_hi, df);
-        const float c_lo = fmaf(k.a_hi, df, -c_hi) + k.a_lo * df;
+        float c_hi, c_lo, e_hi = 0.0f, e_lo = 0.0f, c2_hi = 0.0f, c2_lo = 0.0f, s2_hi = 0.0f, s2_lo = 0.0f;
+        if (!ASTIG) {
+            const float df = defocus[a];
+            // c = alpha * df as hi + lo (the rounded products are __fmul_rn so
+            // that no FMA contraction changes them: the error terms below
+            // assume each one rounded on its own)
+            c_hi = __fmul_rn(k.a_hi, df);
+            c_lo = fmaf(k.a_hi, df, -c_hi) + k.a_lo * df;
+        } else {
+            const double du = defocus[a], dv = defocus_v[a];
+            const double cm = k.alpha * (0.5 * (du + dv)), cd = k.alpha * (0.5 * (du - dv));
+            double sn2, cs2;
+            sincos(2.0 * (double)astig[a], &sn2, &cs2);
+            c_hi = (float)cm;
+            c_lo = (float)(cm - (double)c_hi);
+            e_hi = (float)cd;
+            e_lo = (float)(cd - (double)e_hi);
+            c2_hi = (float)cs2;
+            c2_lo = (float)(cs2 - (double)c2_hi);
+            s2_hi = (float)sn2;
+            s2_lo = (float)(sn2 - (double)s2_hi);
+        }
         const size_t row = ((size_t)a * M + j) * M;
         for (int i = threadIdx.x; i < M; i += kRowX) {
             const int di = i - M / 2;
             const float r2 = (float)(di * di + dj * dj);
             // t1 = r2 * c
-            const float t1_hi = __fmul_rn(r2, c_hi);
-            const float t1_lo = fmaf(r2, c_hi, -t1_hi) + r2 * c_lo;
+            float t1_hi = __fmul_rn(r2, c_hi);
+            float t1_lo = fmaf(r2, c_hi, -t1_hi) + r2 * c_lo;
+            if (ASTIG) {
+                // g = (dx^2 - dy^2) cos 2phi + 2 dx dy sin 2phi, then t1 += e g
+                const float G1 = (float)(di * di - dj * dj), G2 = (float)(2 * di * dj);
+                const float p1 = __fmul_rn(G1, c2_hi), p2 = __fmul_rn(G2, s2_hi);
+                const float e1 = fmaf(G1, c2_hi, -p1) + G1 * c2_lo, e2 = fmaf(G2, s2_hi, -p2) + G2 * s2_lo;
+                const float g_hi = __fadd_rn(p1, p2);
+                const float gb = __fsub_rn(g_hi, p1), ga = __fsub_rn(g_hi, gb);
+                const float g_lo = ((p1 - ga) + (p2 - gb)) + (e1 + e2);
+                const float t3_hi = __fmul_rn(e_hi, g_hi);
+                const float t3_lo = fmaf(e_hi, g_hi, -t3_hi) + e_hi * g_lo + e_lo * g_hi;
+                const float u_hi = __fadd_rn(t1_hi, t3_hi);
+                const float ub = __fsub_rn(u_hi, t1_hi), ua = __fsub_rn(u_hi, ub);
+                t1_lo = ((t1_hi - ua) + (t3_hi - ub)) + (t1_lo + t3_lo);
+                t1_hi = u_hi;
+            }
             // t2 = r2^2 * beta
             const float q_hi = __fmul_rn(r2, r2), q_lo = fmaf(r2, r2, -q_hi);
             const float t2_hi = __fmul_rn(q_hi, k.b_hi);
@@ -594,7 +635,7 @@ static double leading_bits(double x, int bits)
 }
 
 cudaError_t launch_ctf(float *d_mul, int mul_power, float *d_gen, int gen_power, int M, int n, const float *d_defocus,
-                       const CtfParams &c, cudaStream_t s)
+                       const float *d_defocus_v, const float *d_astig, const CtfParams &c, cudaStream_t s)
 {
     if (n <= 0 || (!d_mul && !d_gen)) return cudaSuccess;
     // electron wavelength (Å) at the accelerating voltage, relativistic
@@ -604,6 +645,7 @@ cudaError_t launch_ctf(float *d_mul, int mul_power, float *d_gen, int gen_power,
     const double q = 1.0 / (((double)M * c.pixel_size) * ((double)M * c.pixel_size));
     const double alpha = pi * lambda * q, beta = 0.5 * pi * ((double)c.cs_mm * 1e7) * lambda * lambda * lambda * q * q;
     CtfConsts k;
+    k.alpha = alpha;
     split_f(alpha, &k.a_hi, &k.a_lo);
     split_f(beta, &k.b_hi, &k.b_lo);
     const double p1 = leading_bits(2 * pi, 12), p2 = leading_bits(2 * pi - p1, 12);
@@ -614,7 +656,12 @@ cudaError_t launch_ctf(float *d_mul, int mul_power, float *d_gen, int gen_power,
     const double A = c.amp_contrast;
     k.w_sin = (float)std::sqrt(1.0 - A * A);
     k.w_cos = (float)A;
-    ctf_kernel<<<row_grid(M, n), dim3(kRowX, kRowY), 0, s>>>(d_mul, d_gen, M, n, d_defocus, k, mul_power, gen_power);
+    if (d_defocus_v && d_astig)
+        ctf_kernel<true><<<row_grid(M, n), dim3(kRowX, kRowY), 0, s>>>(d_mul, d_gen, M, n, d_defocus, d_defocus_v,
+                                                                        d_astig, k, mul_power, gen_power);
+    else
+        ctf_kernel<false><<<row_grid(M, n), dim3(kRowX, kRowY), 0, s>>>(d_mul, d_gen, M, n, d_defocus, nullptr,
+                                                                         nullptr, k, mul_power, gen_power);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -873,16 +920,18 @@ extern "C" int gg_filter_complex_to_real(const float *d_complex, float *d_real, 
 }
 
 extern "C" int gg_filter_apply_ctf(float *d_cas_images, int cas_img_size, int n_images, const float *d_defocus,
-                                   float voltage_kv, float cs_mm, float amp_contrast, float pixel_size, int power,
-                                   int generate, void *stream)
+                                   const float *d_defocus_v, const float *d_astig_angle, float voltage_kv, float cs_mm,
+                                   float amp_contrast, float pixel_size, int power, int generate, void *stream)
 {
     if (cas_img_size <= 0 || n_images < 0 || (n_images > 0 && (!d_cas_images || !d_defocus)) ||
         (power != 1 && power != 2) || !(voltage_kv > 0.0f) || !(pixel_size > 0.0f) ||
-        !(amp_contrast >= 0.0f && amp_contrast <= 1.0f) || !std::isfinite(cs_mm))
+        !(amp_contrast >= 0.0f && amp_contrast <= 1.0f) || !std::isfinite(cs_mm) ||
+        ((d_defocus_v == nullptr) != (d_astig_angle == nullptr)))
         return GG_ERR_INVALID_ARG;
     const CtfParams c{voltage_kv, cs_mm, amp_contrast, pixel_size};
     return launch_ctf(generate ? nullptr : d_cas_images, power, generate ? d_cas_images : nullptr, power,
-                      cas_img_size, n_images, d_defocus, c, (cudaStream_t)stream) == cudaSuccess
+                      cas_img_size, n_images, d_defocus, d_defocus_v, d_astig_angle, c, (cudaStream_t)stream) ==
+                   cudaSuccess
                ? GG_OK
                : GG_ERR_CUDA;
 }

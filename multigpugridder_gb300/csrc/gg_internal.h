@@ -137,12 +137,15 @@ struct CtfParams {
 // Constants of the CTF kernel: alpha, beta as float pairs, 2 pi in three
 // parts for the reduction, the sin / cos weights.
 struct CtfConsts {
+    double alpha; // pi lambda / (M px)^2 (FP64, for the astigmatic terms)
     float a_hi, a_lo, b_hi, b_lo, p1, p2, p3, inv_2pi, w_sin, w_cos;
 };
-// Over n CAS images of M x M (d_defocus: n defoci in Å): d_mul (optional)
-// *= CTF^mul_power and d_gen (optional) = CTF^gen_power, in one pass.
+// Over n CAS images of M x M (d_defocus: n defoci in Å; with d_defocus_v and
+// d_astig both given, defocus U / V and the astigmatism angle in radians):
+// d_mul (optional) *= CTF^mul_power and d_gen (optional) = CTF^gen_power, in
+// one pass.
 cudaError_t launch_ctf(float *d_mul, int mul_power, float *d_gen, int gen_power, int M, int n, const float *d_defocus,
-                       const CtfParams &c, cudaStream_t s);
+                       const float *d_defocus_v, const float *d_astig, const CtfParams &c, cudaStream_t s);
 
 // ---- fused 2-D FFT stages (gg_fft2.cu) ----------------------------------------
 // True when N, M take the fused kernels: M in {64, 128, 256}, N <= M/2, N a

@@ -262,22 +262,34 @@ class MultiGPUGridder:
         return out
 
     def reconstructVolCTF(self, images, axes, defocus, voltage_kv=300.0, cs_mm=2.7, amp_contrast=0.1,
-                          pixel_size=1.0):
+                          pixel_size=1.0, defocus_v=None, astig_angle=None):
         """reconstructVol with each image's weak-phase CTF applied before the
         back projection (the reference's unimplemented ApplyCTFs flag,
         src/Gridders/AbstractGridder.h:118-119): the CAS images are multiplied
         by the CTF and the plane density back-projects CTF^2.  defocus: one
-        value per image in Å (underfocus positive); cs_mm in mm; pixel_size in
-        Å per image pixel."""
+        value per image in Å (underfocus positive; defocus U when astigmatic);
+        defocus_v, astig_angle: per-image defocus V (Å) and the angle of the U
+        axis from the image x axis (radians), both or neither; cs_mm in mm;
+        pixel_size in Å per image pixel."""
         self.Images = _own(images)
         self.coordAxes = self._axes(axes)
         ax = self._axes(self.coordAxes)
-        df = np.ascontiguousarray(defocus, dtype=np.float32).reshape(-1)
-        if df.size != ax.shape[0]:
-            raise ValueError("defocus needs one value per image (%d), got %d" % (ax.shape[0], df.size))
+        n_img = ax.shape[0]
+
+        def per_image(x, name):
+            v = np.ascontiguousarray(x, dtype=np.float32).reshape(-1)
+            if v.size != n_img:
+                raise ValueError("%s needs one value per image (%d), got %d" % (name, n_img, v.size))
+            return v
+
+        df = per_image(defocus, "defocus")
+        if (defocus_v is None) != (astig_angle is None):
+            raise ValueError("defocus_v and astig_angle go together")
+        dv = per_image(defocus_v, "defocus_v") if defocus_v is not None else None
+        an = per_image(astig_angle, "astig_angle") if astig_angle is not None else None
         n = self.VolumeSize
         out = np.empty((n, n, n), dtype=np.float32)
-        self._call("gg_reconstruct_volume_ctf", _ptr(ax), ax.shape[0], _ptr(self.Images), _ptr(df),
+        self._call("gg_reconstruct_volume_ctf", _ptr(ax), n_img, _ptr(self.Images), _ptr(df), _ptr(dv), _ptr(an),
                    float(voltage_kv), float(cs_mm), float(amp_contrast), float(pixel_size), _ptr(out))
         self.Volume = out
         self._cas_from_volume = False

@@ -410,26 +410,38 @@ def electron_wavelength(voltage_kv):
     return 12.2643247 / math.sqrt(U * (1.0 + 0.978466e-6 * U))
 
 
-def ctf_cas(M, defocus, voltage_kv, cs_mm, amp_contrast, pixel_size):
+def ctf_cas(M, defocus, voltage_kv, cs_mm, amp_contrast, pixel_size, defocus_v=None, astig_angle=None):
     """Weak-phase CTF on the CAS-image grid, FP64, shape (n, M, M), DC at
     (M/2, M/2).  No reference counterpart (the reference declares only the
     ApplyCTFs flag, src/Gridders/AbstractGridder.h:118-119):
     CTF = -(sqrt(1 - A^2) sin chi + A cos chi),
-    chi = pi lambda df s^2 - pi/2 Cs lambda^3 s^4, s = |(i, j) - M/2| / (M px)."""
+    chi = pi lambda df s^2 - pi/2 Cs lambda^3 s^4, s = |(i, j) - M/2| / (M px).
+    Astigmatic (defocus_v, astig_angle given): defocus is U and
+    df = (U + V)/2 + (U - V)/2 cos 2(theta - angle), theta the angle of the
+    frequency (i - M/2, j - M/2) from the x axis."""
     lam = electron_wavelength(voltage_kv)
     f = (np.arange(M) - M // 2) / (M * float(pixel_size))
-    s2 = f[None, :] ** 2 + f[:, None] ** 2
-    df = np.asarray(defocus, dtype=np.float64).reshape(-1, 1, 1)
+    fx, fy = f[None, :], f[:, None]
+    s2 = fx ** 2 + fy ** 2
+    du = np.asarray(defocus, dtype=np.float64).reshape(-1, 1, 1)
+    if defocus_v is None:
+        df = du
+    else:
+        dv = np.asarray(defocus_v, dtype=np.float64).reshape(-1, 1, 1)
+        ang = np.asarray(astig_angle, dtype=np.float64).reshape(-1, 1, 1)
+        theta = np.arctan2(np.broadcast_to(fy, s2.shape), np.broadcast_to(fx, s2.shape))[None]
+        df = 0.5 * (du + dv) + 0.5 * (du - dv) * np.cos(2.0 * (theta - ang))
     chi = math.pi * lam * df * s2 - 0.5 * math.pi * (cs_mm * 1e7) * lam ** 3 * s2 ** 2
     A = float(amp_contrast)
     return -(math.sqrt(1.0 - A * A) * np.sin(chi) + A * np.cos(chi))
 
 
-def reconstruct_vol_ctf(imgs, axes, p, defocus, voltage_kv, cs_mm, amp_contrast, pixel_size, precision="f64"):
+def reconstruct_vol_ctf(imgs, axes, p, defocus, voltage_kv, cs_mm, amp_contrast, pixel_size, precision="f64",
+                        defocus_v=None, astig_angle=None):
     """reconstructVol with the CTF applied to each CAS image before the back
     projection and CTF^2 images as the plane density:
     volFromCAS(BP(CTF . CAS(img)) ./ (BP(CTF^2) + 1e-6))."""
-    c = ctf_cas(p.M, defocus, voltage_kv, cs_mm, amp_contrast, pixel_size)
+    c = ctf_cas(p.M, defocus, voltage_kv, cs_mm, amp_contrast, pixel_size, defocus_v, astig_angle)
     if precision == "f32":
         c = c.astype(np.float32).astype(np.float64)
     ci = cas_imgs_from_imgs(imgs, p.M) * c

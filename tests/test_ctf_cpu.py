@@ -46,3 +46,21 @@ def test_ctf_corrected_reconstruction_reduces_to_plain():
     plain = O.reconstruct_vol(imgs, axes, p)[0]
     ctf = O.reconstruct_vol_ctf(imgs, axes, p, np.zeros(len(axes)), 300.0, 0.0, 1.0, 1.0)[0]
     assert np.allclose(ctf, -plain, rtol=0, atol=1e-12 * np.abs(plain).max())
+
+
+def test_astigmatic_ctf_reduces_and_is_symmetric():
+    M, px, A = 64, 1.2, 0.1
+    u = [15000.0, 9000.0]
+    v = [12000.0, 9000.0]
+    ang = [0.3, -1.1]
+    c = O.ctf_cas(M, u, 300.0, 2.7, A, px, v, ang)
+    # V = U: the isotropic CTF
+    assert np.array_equal(O.ctf_cas(M, u, 300.0, 2.7, A, px, u, ang), O.ctf_cas(M, u, 300.0, 2.7, A, px))
+    # the angle is defined modulo pi, and (U, V, a) equals (V, U, a + pi/2)
+    c_pi = O.ctf_cas(M, u, 300.0, 2.7, A, px, v, np.add(ang, math.pi))
+    c_sw = O.ctf_cas(M, v, 300.0, 2.7, A, px, u, np.add(ang, math.pi / 2))
+    assert np.allclose(c_pi, c, rtol=0, atol=1e-9) and np.allclose(c_sw, c, rtol=0, atol=1e-9)
+    # along the U axis the defocus is U: pixel (M/2 + 10, M/2) with angle 0
+    cu = O.ctf_cas(M, [u[0]], 300.0, 2.7, A, px, [v[0]], [0.0])[0]
+    iso = O.ctf_cas(M, [u[0]], 300.0, 2.7, A, px)[0]
+    assert abs(cu[M // 2, M // 2 + 10] - iso[M // 2, M // 2 + 10]) < 1e-12

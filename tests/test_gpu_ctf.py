@@ -43,7 +43,7 @@ def test_ctf_filter_matches_formula(cuda, gglib, M, px):
     ref = O.ctf_cas(M, df, KV, CS, AMP, px)
     for power in (1, 2):
         out = torch.full((n, M, M), float("nan"), device=cuda)
-        assert gglib.gg_filter_apply_ctf(dptr(out), M, n, dptr(d_df), KV, CS, AMP, px, power, 1, None) == 0
+        assert gglib.gg_filter_apply_ctf(dptr(out), M, n, dptr(d_df), None, None, KV, CS, AMP, px, power, 1, None) == 0
         torch.cuda.synchronize()
         got = out.cpu().numpy().astype(np.float64)
         assert np.max(np.abs(got - ref ** power)) < 1e-6
@@ -51,8 +51,8 @@ def test_ctf_filter_matches_formula(cuda, gglib, M, px):
     img = np.random.default_rng(M).standard_normal((n, M, M)).astype(np.float32)
     d_img = to_dev(img, cuda)
     gen = torch.empty_like(d_img)
-    assert gglib.gg_filter_apply_ctf(dptr(d_img), M, n, dptr(d_df), KV, CS, AMP, px, 1, 0, None) == 0
-    assert gglib.gg_filter_apply_ctf(dptr(gen), M, n, dptr(d_df), KV, CS, AMP, px, 1, 1, None) == 0
+    assert gglib.gg_filter_apply_ctf(dptr(d_img), M, n, dptr(d_df), None, None, KV, CS, AMP, px, 1, 0, None) == 0
+    assert gglib.gg_filter_apply_ctf(dptr(gen), M, n, dptr(d_df), None, None, KV, CS, AMP, px, 1, 1, None) == 0
     torch.cuda.synchronize()
     assert np.array_equal(d_img.cpu().numpy(), img * gen.cpu().numpy())
 
@@ -64,11 +64,11 @@ def test_ctf_filter_rejects_bad_parameters(cuda, gglib):
 
     x = torch.zeros((1, 8, 8), device=cuda)
     d = torch.zeros(1, device=cuda)
-    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 1, dptr(d), 0.0, CS, AMP, 1.0, 1, 0, None) == GG_ERR_INVALID_ARG
-    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 1, dptr(d), KV, CS, 1.5, 1.0, 1, 0, None) == GG_ERR_INVALID_ARG
-    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 1, dptr(d), KV, CS, AMP, 0.0, 1, 0, None) == GG_ERR_INVALID_ARG
-    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 1, dptr(d), KV, CS, AMP, 1.0, 3, 0, None) == GG_ERR_INVALID_ARG
-    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 0, None, KV, CS, AMP, 1.0, 1, 0, None) == 0
+    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 1, dptr(d), None, None, 0.0, CS, AMP, 1.0, 1, 0, None) == GG_ERR_INVALID_ARG
+    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 1, dptr(d), None, None, KV, CS, 1.5, 1.0, 1, 0, None) == GG_ERR_INVALID_ARG
+    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 1, dptr(d), None, None, KV, CS, AMP, 0.0, 1, 0, None) == GG_ERR_INVALID_ARG
+    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 1, dptr(d), None, None, KV, CS, AMP, 1.0, 3, 0, None) == GG_ERR_INVALID_ARG
+    assert gglib.gg_filter_apply_ctf(dptr(x), 8, 0, None, None, None, KV, CS, AMP, 1.0, 1, 0, None) == 0
 
 
 def _data(N, n, seed):
@@ -146,9 +146,54 @@ def test_ctf_reconstruction_device_form_equals_host_form(cuda):
         out = torch.empty((N, N, N), device=cuda)
         d_ax, d_im, d_df = to_dev(axes, cuda), to_dev(imgs, cuda), to_dev(df, cuda)
         s = torch.cuda.current_stream(cuda)
-        check(lib().gg_reconstruct_volume_ctf_dev(g.handle, dptr(d_ax), len(axes), dptr(d_im), dptr(d_df), KV, CS,
-                                                  AMP, 1.2, dptr(out), ctypes.c_void_p(s.cuda_stream)), g.handle)
+        check(lib().gg_reconstruct_volume_ctf_dev(g.handle, dptr(d_ax), len(axes), dptr(d_im), dptr(d_df), None,
+                                                  None, KV, CS, AMP, 1.2, dptr(out), ctypes.c_void_p(s.cuda_stream)),
+              g.handle)
         torch.cuda.synchronize()
         assert np.array_equal(out.cpu().numpy(), host)
         with pytest.raises(ValueError):
             g.reconstructVolCTF(imgs, axes, df[:-1])
+
+
+@pytest.mark.parametrize("M,px", [(64, 1.5), (256, 1.0)])
+def test_astigmatic_ctf_filter_matches_formula(cuda, gglib, M, px):
+    import torch
+
+    rng = np.random.default_rng(M + 1)
+    n = 6
+    du = rng.uniform(5000.0, 40000.0, n).astype(np.float32)
+    dv = (du - rng.uniform(-3000.0, 3000.0, n)).astype(np.float32)
+    ang = rng.uniform(-np.pi, np.pi, n).astype(np.float32)
+    ref = O.ctf_cas(M, du, KV, CS, AMP, px, dv, ang)
+    out = torch.full((n, M, M), float("nan"), device=cuda)
+    d_u, d_v, d_a = to_dev(du, cuda), to_dev(dv, cuda), to_dev(ang, cuda)
+    assert gglib.gg_filter_apply_ctf(dptr(out), M, n, dptr(d_u), dptr(d_v), dptr(d_a), KV, CS, AMP, px, 1, 1,
+                                     None) == 0
+    torch.cuda.synchronize()
+    assert np.max(np.abs(out.cpu().numpy().astype(np.float64) - ref)) < 1e-6
+    # V without an angle is refused
+    from multigpugridder_gb300._lib import GG_ERR_INVALID_ARG
+    assert gglib.gg_filter_apply_ctf(dptr(out), M, n, dptr(d_u), dptr(d_v), None, KV, CS, AMP, px, 1, 1,
+                                     None) == GG_ERR_INVALID_ARG
+
+
+def test_astigmatic_ctf_reconstruction_matches_oracle(cuda):
+    import multigpugridder_gb300 as gg
+
+    N = 32
+    p = O.Params(N)
+    vol, axes = _data(N, 30, 90)
+    rng = np.random.default_rng(91)
+    du = rng.uniform(6000.0, 25000.0, len(axes)).astype(np.float32)
+    dv = (du - rng.uniform(-2000.0, 2000.0, len(axes))).astype(np.float32)
+    ang = rng.uniform(0.0, np.pi, len(axes)).astype(np.float32)
+    with gg.MultiGPUGridder(N, len(axes), adjustInterpFactor=False) as g:
+        g.setVolume(vol)
+        imgs = g.forwardProject(axes)
+        rec = g.reconstructVolCTF(imgs, axes, du, KV, CS, AMP, 2.0, defocus_v=dv, astig_angle=ang)
+        with pytest.raises(ValueError):
+            g.reconstructVolCTF(imgs, axes, du, defocus_v=dv)
+    ref = O.reconstruct_vol_ctf(imgs, axes, p, du, KV, CS, AMP, 2.0, precision="f32", defocus_v=dv,
+                                astig_angle=ang)[0]
+    assert O.rel_l2(rec, ref) < TOL
+
