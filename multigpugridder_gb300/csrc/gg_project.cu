@@ -347,7 +347,7 @@ cudaError_t launch_forward_project(const void *d_vol, int vprec, int pitch, floa
 // ---------------------------------------------------------------------------
 // Directions are staged through shared memory in chunks of kBpChunk, one per
 // thread of a CTA for the cull.
-constexpr int kBpChunk = 256;
+constexpr int kBpChunk = 512;
 
 // Conservative reach of the slab test: fp32 rounding of f_imgk is far below this.
 constexpr float kCullEps = 1e-2f;
@@ -420,7 +420,7 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
 // the per-voxel sums are those of the reference kernel's loops, bit for bit.
 constexpr int kCBX = 16, kCBY = 8; // brick: 2x2x2 warp blocks of 8x4xBD (BD = 8, or 4 for ADJ / DW)
 constexpr int kCThreads = 256;
-static_assert(kBpChunk == kCThreads, "the cull compaction gives one direction per thread");
+static_assert(kBpChunk % kCThreads == 0, "the cull gives each thread kBpChunk / kCThreads directions");
 // Depth of a warp block for the reference rule: 6 voxels, or 8 (DEEP) on CAS
 // images of 512^2 and more.  Deeper blocks have more active voxels per
 // direction (fewer idle lanes in the last round of 32) and stage a footprint
@@ -634,7 +634,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     extern __shared__ float stab[]; // (kerSize + 2 tabPad) entries x kTabRep copies
     __shared__ float sax[kBpChunk * 9];
     __shared__ int slist[kBpChunk];
-    __shared__ int swarp[kBpChunk / 32];
+    __shared__ int swarp[kBpChunk / 32]; // kept directions per (pass, warp)
     __shared__ int scount;
     // per-voxel sums [warp][block voxel]; a voxel is updated by at most one
     // lane per direction, directions in order, so no atomics are needed
@@ -704,37 +704,50 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         __syncthreads();
         for (int t = tid; t < cn * 9; t += kCThreads) sax[t] = __ldg(axes + (size_t)c0 * 9 + t);
         __syncthreads();
-        bool keep = false;
-        int ortho = 0;
-        if (tid < cn) {
-            const float *ax = sax + tid * 9;
-            const float zx = ax[6], zy = ax[7], zz = ax[8];
-            const float d = bcx * zx + bcy * zy + bcz * zz;
-            const float ext = 0.5f * ((kCBX - 1) * fabsf(zx) + (kCBY - 1) * fabsf(zy) + (kCBZ - 1) * fabsf(zz));
-            keep = fabsf(d) <= slab + ext;
-            // the fast window needs orthonormal axes (they bound |Q - v|);
-            // NaN or infinite entries fail these tests
-            const float xx = ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2];
-            const float yy = ax[3] * ax[3] + ax[4] * ax[4] + ax[5] * ax[5];
-            const float zz2 = zx * zx + zy * zy + zz * zz;
-            const float xy = ax[0] * ax[3] + ax[1] * ax[4] + ax[2] * ax[5];
-            const float xz = ax[0] * zx + ax[1] * zy + ax[2] * zz;
-            const float yz = ax[3] * zx + ax[4] * zy + ax[5] * zz;
-            ortho = (fabsf(xx - 1.0f) <= 1e-3f && fabsf(yy - 1.0f) <= 1e-3f && fabsf(zz2 - 1.0f) <= 1e-3f &&
-                     fabsf(xy) <= 1e-3f && fabsf(xz) <= 1e-3f && fabsf(yz) <= 1e-3f) ? kBpChunk : 0;
+        // cull: thread tid takes directions tid + p * kCThreads; the kept
+        // ones are listed in direction order (pass by pass, warp by warp)
+        constexpr int kPasses = kBpChunk / kCThreads;
+        unsigned ballots[kPasses];
+        bool keeps[kPasses];
+        int orthos[kPasses];
+#pragma unroll
+        for (int pss = 0; pss < kPasses; pss++) {
+            const int d = tid + pss * kCThreads;
+            bool keep = false;
+            int ortho = 0;
+            if (d < cn) {
+                const float *ax = sax + d * 9;
+                const float zx = ax[6], zy = ax[7], zz = ax[8];
+                const float dd = bcx * zx + bcy * zy + bcz * zz;
+                const float ext = 0.5f * ((kCBX - 1) * fabsf(zx) + (kCBY - 1) * fabsf(zy) + (kCBZ - 1) * fabsf(zz));
+                keep = fabsf(dd) <= slab + ext;
+                // the fast window needs orthonormal axes (they bound |Q - v|);
+                // NaN or infinite entries fail these tests
+                const float xx = ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2];
+                const float yy = ax[3] * ax[3] + ax[4] * ax[4] + ax[5] * ax[5];
+                const float zz2 = zx * zx + zy * zy + zz * zz;
+                const float xy = ax[0] * ax[3] + ax[1] * ax[4] + ax[2] * ax[5];
+                const float xz = ax[0] * zx + ax[1] * zy + ax[2] * zz;
+                const float yz = ax[3] * zx + ax[4] * zy + ax[5] * zz;
+                ortho = (fabsf(xx - 1.0f) <= 1e-3f && fabsf(yy - 1.0f) <= 1e-3f && fabsf(zz2 - 1.0f) <= 1e-3f &&
+                         fabsf(xy) <= 1e-3f && fabsf(xz) <= 1e-3f && fabsf(yz) <= 1e-3f) ? kBpChunk : 0;
+            }
+            keeps[pss] = keep;
+            orthos[pss] = ortho;
+            ballots[pss] = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0) swarp[pss * (kCThreads / 32) + warp] = __popc(ballots[pss]);
         }
-        const unsigned ballot = __ballot_sync(0xffffffffu, keep);
-        if (lane == 0) swarp[warp] = __popc(ballot);
         __syncthreads();
         {
             int off = 0;
-            for (int w = 0; w < warp; w++) off += swarp[w];
-            if (keep) slist[off + __popc(ballot & lt_mask)] = tid | ortho;
-            if (tid == kCThreads - 1) {
-                int tot = 0;
-                for (int w = 0; w < kCThreads / 32; w++) tot += swarp[w];
-                scount = tot;
+#pragma unroll
+            for (int pss = 0; pss < kPasses; pss++) {
+                int o = off;
+                for (int w = 0; w < warp; w++) o += swarp[pss * (kCThreads / 32) + w];
+                if (keeps[pss]) slist[o + __popc(ballots[pss] & lt_mask)] = (tid + pss * kCThreads) | orthos[pss];
+                for (int w = 0; w < kCThreads / 32; w++) off += swarp[pss * (kCThreads / 32) + w];
             }
+            if (tid == kCThreads - 1) scount = off;
         }
         __syncthreads();
         const int count = scount;
