@@ -53,9 +53,9 @@ cudaError_t launch_pitch_volume(const float *d_cas, int V, int P, void *d_out, i
                                 cudaStream_t s, int layout = 0);
 
 // Back projection with the reference window rule, accumulated (+=) into the
-// FP32 CAS volume.  d_img holds n*M*M FP32 CAS images (iprec kF32; other
-// values are refused); when `ones` is set the images are taken to be all
-// ones (plane density) and d_img is not read.
+// FP32 CAS volume.  d_img holds n*M*M CAS images in storage `iprec`; when
+// `ones` is set the images are taken to be all ones (plane density) and
+// d_img is not read.
 // *d_scale multiplies each voxel's sum before it is added.
 cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, bool ones,
                                     const float *d_ker, const float *d_axes, int n, const Geom &g,

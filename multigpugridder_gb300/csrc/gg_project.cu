@@ -915,21 +915,28 @@ static cudaError_t launch_bp_ref_sized(float *vol, const TI *img, const float *k
     return launch_bp_compact_t<TI, ONES, DENS>(vol, img, ker, axes, n, g, scale, s, pd);
 }
 
-// The back projection reads FP32 CAS images (iprec kF32) in every storage
-// mode; the kernels' image type stays a template parameter.
 cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, bool ones, const float *d_ker,
                                     const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
 {
     if (ones) return launch_bp_ref_sized<float, true, false>(d_vol, nullptr, d_ker, d_axes, n, g, scale, s);
-    if (iprec != kF32) return cudaErrorInvalidValue;
-    return launch_bp_ref_sized<float, false, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF32)
+        return launch_bp_ref_sized<float, false, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
+    if (iprec == kF16)
+        return launch_bp_ref_sized<__half, false, false>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
+    return launch_bp_ref_sized<__nv_bfloat16, false, false>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g,
+                                                            scale, s);
 }
 
 cudaError_t launch_back_project_ref_density(float *d_vol, float *d_pd, const void *d_img, int iprec, const float *d_ker,
                                             const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
 {
-    if (iprec != kF32) return cudaErrorInvalidValue;
-    return launch_bp_ref_sized<float, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
+    if (iprec == kF32)
+        return launch_bp_ref_sized<float, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s, d_pd);
+    if (iprec == kF16)
+        return launch_bp_ref_sized<__half, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s,
+                                                        d_pd);
+    return launch_bp_ref_sized<__nv_bfloat16, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g,
+                                                           scale, s, d_pd);
 }
 
 cudaError_t launch_back_project_ref_pair(float *d_vol, float *d_pd, const float *d_img, const float *d_img2,
@@ -943,9 +950,14 @@ cudaError_t launch_back_project_adjoint(float *d_vol, const void *d_img, int ipr
                                         const float *d_axes, int n, const Geom &g, const float *scale, bool zero_edges,
                                         cudaStream_t s)
 {
-    if (iprec != kF32) return cudaErrorInvalidValue;
-    return launch_bp_compact_t<float, false, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s,
-                                                           nullptr, zero_edges);
+    if (iprec == kF32)
+        return launch_bp_compact_t<float, false, false, true>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s,
+                                                               nullptr, zero_edges);
+    if (iprec == kF16)
+        return launch_bp_compact_t<__half, false, false, true>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale,
+                                                                s, nullptr, zero_edges);
+    return launch_bp_compact_t<__nv_bfloat16, false, false, true>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n,
+                                                                   g, scale, s, nullptr, zero_edges);
 }
 
 } // namespace gg
