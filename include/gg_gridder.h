@@ -44,10 +44,8 @@ extern "C" {
 #define GG_ERR_CUFFT 6
 #define GG_ERR_TIMEOUT 7 /* gg_server_wait: the request is not done yet */
 
-/* storage precision of the resident CAS volume that the forward projection
-   reads (window accumulation is always FP32).  The back projection reads FP32
-   CAS images in every mode: it is not bandwidth-bound, and 2-byte images made
-   it slower. */
+/* storage precision of the resident CAS volume and of the CAS images the
+   projection kernels read (window accumulation is always FP32) */
 #define GG_PREC_F32 0
 #define GG_PREC_F16 1
 #define GG_PREC_BF16 2
@@ -89,7 +87,7 @@ int gg_set_mask_radius(gg_gridder *h, float radius);                /* SetMaskRa
 int gg_set_max_axes_to_allocate(gg_gridder *h, int max_axes);       /* SetMaxAxesToAllocate: directions per device batch */
 int gg_set_num_streams_fp(gg_gridder *h, int n);                    /* SetNumStreamsFP: copy/compute pipeline depth */
 int gg_set_num_streams_bp(gg_gridder *h, int n);                    /* SetNumStreamsBP */
-int gg_set_precision(gg_gridder *h, int precision);                 /* GG_PREC_*: storage of the resident CAS volume */
+int gg_set_precision(gg_gridder *h, int precision);                 /* GG_PREC_*: storage of CAS volume / CAS images */
 int gg_set_bp_mode(gg_gridder *h, int mode);                        /* GG_BP_REF (default) or GG_BP_ADJOINT */
 
 /* setVolume + the CAS preparation of forwardProject

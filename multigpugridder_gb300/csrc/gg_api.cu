@@ -165,6 +165,7 @@ struct gg_gridder {
     struct Slot {
         DevBuf<float> casimg, real, img;
         DevBuf<cufftComplex> spec;
+        DevBuf<uint16_t> casimg_lp;
         PinBuf stage;
         cudaEvent_t ev_ready = nullptr, ev_free = nullptr;
     } slot[2];
@@ -186,6 +187,7 @@ struct gg_gridder {
 
     Geom geom() const { return Geom{V, M, mask_radius, ker_size, ker_hw}; }
     const float *vol_scale() const { return prec == kF16 ? scales.p : nullptr; }
+    const float *img_scale() const { return prec == kF16 ? scales.p + 1 : nullptr; }
 };
 
 namespace {
@@ -232,6 +234,7 @@ void ensure_slot(gg_gridder *h, int s, int b, bool need_img)
     sl.real.ensure(MM * b);
     sl.spec.ensure(H * b);
     if (need_img) sl.img.ensure(NN * b);
+    if (h->prec != kF32) sl.casimg_lp.ensure(MM * b);
     if (!sl.ev_ready) GG_CK(cudaEventCreateWithFlags(&sl.ev_ready, cudaEventDisableTiming));
     if (!sl.ev_free) {
         GG_CK(cudaEventCreateWithFlags(&sl.ev_free, cudaEventDisableTiming));
@@ -385,27 +388,49 @@ void fp_batch(gg_gridder *h, const float *d_axes, int b, float *cas_out, float *
 void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const float *casimg, float *target, bool ones,
               int sl, cudaStream_t s, float *pd = nullptr)
 {
-    // The back projection reads FP32 CAS images in every storage mode: it is
-    // not bandwidth-bound, and with 2-byte images it measured 5-9% slower.
     auto &S = h->slot[sl];
     const void *src = nullptr;
-    const int iprec = kF32;
+    int iprec = h->prec;
     const float *scale = nullptr;
     if (!ones) {
+        const size_t MM = (size_t)h->M * h->M;
         if (casimg) {
-            src = casimg;
+            if (h->prec == kF32) {
+                src = casimg;
+            } else {
+                if (h->prec == kF16) GG_CK(launch_storage_scale(casimg, MM * b, 8192.0f, h->work.p, h->scales.p + 1, s));
+                GG_CK(launch_convert(casimg, S.casimg_lp.p, h->prec, MM * b, h->img_scale(), s));
+                src = S.casimg_lp.p;
+                scale = h->img_scale();
+            }
+        } else if (h->fused_fft && h->prec != kF16) {
+            void *dst = h->prec == kF32 ? (void *)S.casimg.p : (void *)S.casimg_lp.p;
+            GG_CK(launch_images_to_cas_fused(img, h->N, h->M, b, dst, h->prec, false, s));
+            src = dst;
         } else if (h->fused_fft) {
+            // FP16: FP32 CAS images first, then the storage scale from their
+            // largest magnitude and the conversion
             GG_CK(launch_images_to_cas_fused(img, h->N, h->M, b, S.casimg.p, kF32, false, s));
-            src = S.casimg.p;
+            GG_CK(launch_storage_scale(S.casimg.p, MM * b, 8192.0f, h->work.p, h->scales.p + 1, s));
+            GG_CK(launch_convert(S.casimg.p, S.casimg_lp.p, h->prec, MM * b, h->img_scale(), s));
+            src = S.casimg_lp.p;
+            scale = h->img_scale();
         } else {
             GG_CK(launch_images_to_fft_input(img, h->N, h->M, b, S.real.p, s));
             cufftHandle p = plan2d(h, CUFFT_R2C, b);
             GG_CKF(cufftSetStream(p, s));
             GG_CKF(cufftExecR2C(p, S.real.p, S.spec.p));
-            GG_CK(launch_spectrum_to_cas_images(S.spec.p, h->M, b, S.casimg.p, kF32, nullptr, s));
-            src = S.casimg.p;
+            if (h->prec == kF16)
+                // |Re + Im| <= 2 max(|Re|, |Im|)
+                GG_CK(launch_storage_scale((const float *)S.spec.p, (size_t)h->M * (h->M / 2 + 1) * 2 * b, 4096.0f,
+                                           h->work.p, h->scales.p + 1, s));
+            void *dst = h->prec == kF32 ? (void *)S.casimg.p : (void *)S.casimg_lp.p;
+            GG_CK(launch_spectrum_to_cas_images(S.spec.p, h->M, b, dst, h->prec, h->img_scale(), s));
+            src = dst;
+            scale = h->img_scale();
         }
     }
+    if (ones) iprec = kF32;
     ProfScope ps(h, s, ones ? GG_KERNEL_DENSITY : GG_KERNEL_BACK);
     if (h->bp_mode == GG_BP_ADJOINT && !ones) {
         GG_CK(launch_back_project_adjoint(target, src, iprec, h->ker.p, d_axes, b, h->geom(), scale, !h->five_taps, s));
@@ -444,7 +469,7 @@ void ctf_batch(gg_gridder *h, const float *d_axes, int b, const float *img, cons
     }
     // CAS images *= CTF, and CTF^2 into S.real (free after the R2C), in one pass
     GG_CK(launch_ctf(S.casimg.p, 1, S.real.p, 2, h->M, b, d_defocus, d_defocus_v, d_astig, c, s));
-    if (h->bp_mode != GG_BP_ADJOINT) {
+    if (h->prec == kF32 && h->bp_mode != GG_BP_ADJOINT) {
         // both stacks in one back-projection pass
         ProfScope ps(h, s, GG_KERNEL_BACK);
         GG_CK(launch_back_project_ref_pair(h->cas.p, h->pd.p, S.casimg.p, S.real.p, h->ker.p, d_axes, b, h->geom(), s));
@@ -658,6 +683,7 @@ void destroy_handle(gg_gridder *h)
         S.real.release();
         S.img.release();
         S.spec.release();
+        S.casimg_lp.release();
         S.stage.release();
         if (S.ev_ready) cudaEventDestroy(S.ev_ready);
         if (S.ev_free) cudaEventDestroy(S.ev_free);
@@ -870,6 +896,7 @@ extern "C" int gg_set_precision(gg_gridder *h, int precision)
             GG_CK(cudaStreamSynchronize(h->cs));
             h->prec = precision;
             h->cas_fp_valid = false;
+            for (auto &S : h->slot) S.casimg_lp.release();
         }
     });
 }

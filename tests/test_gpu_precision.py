@@ -1,6 +1,5 @@
-"""Reduced-precision storage (FP16 / BF16 resident CAS volume read by the
-forward projection; FP32 CAS images for the back projection and FP32 window
-accumulation in every mode) against the FP64 oracle.
+"""Reduced-precision storage (FP16 / BF16 CAS volume and CAS images, FP32
+window accumulation) against the FP64 oracle.
 
 Bound: relative L2 <= 1e-3 against FP64 for every stored form; the FP32 path
 is also checked against FP64 (it differs only by FP32 rounding, which can move
