@@ -496,8 +496,11 @@ def run_precision(args):
     def vp(t):
         return ctypes.c_void_p(t.data_ptr())
 
-    for prec in ("f32", "bf16", "f16"):
-        g = gg.MultiGPUGridder(N, n, 2.0, MaxAxesToAllocate=1000, precision=prec)
+    # "bf16_vol": BF16 volume, FP32 CAS images for the back projection
+    for prec in ("f32", "bf16", "f16", "bf16_vol"):
+        g = gg.MultiGPUGridder(N, n, 2.0, MaxAxesToAllocate=1000, precision="bf16" if prec == "bf16_vol" else prec)
+        if prec == "bf16_vol":
+            g.set_image_precision("f32")
         h = g.handle
         imgs = torch.empty((n, N, N), dtype=torch.float32, device=dev)
         rec = torch.empty((N, N, N), dtype=torch.float32, device=dev)
@@ -526,8 +529,8 @@ def run_precision(args):
         g.close()
         del imgs, rec
     return {"workload": "256^3 volume (400 blobs), interpFactor 2 (CAS volume 518^3), 5,000 random-quaternion "
-                        "directions: setVolume + forwardProject + reconstructVol, storage f32/bf16/f16, FP32 "
-                        "accumulation", "results": out}
+                        "directions: setVolume + forwardProject + reconstructVol, storage f32/bf16/f16 (volume and "
+                        "CAS images) and bf16_vol (BF16 volume, FP32 CAS images), FP32 accumulation", "results": out}
 
 
 # ---- differentiation -----------------------------------------------------------

@@ -54,6 +54,7 @@ SIGNATURES = {
     "gg_set_num_streams_fp": (_c_int, [_vp, _c_int]),
     "gg_set_num_streams_bp": (_c_int, [_vp, _c_int]),
     "gg_set_precision": (_c_int, [_vp, _c_int]),
+    "gg_set_image_precision": (_c_int, [_vp, _c_int]),
     "gg_set_bp_mode": (_c_int, [_vp, _c_int]),
     "gg_set_volume": (_c_int, [_vp, _fp, _ip]),
     "gg_set_cas_volume": (_c_int, [_vp, _fp, _ip]),

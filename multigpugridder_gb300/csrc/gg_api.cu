@@ -140,7 +140,8 @@ struct gg_gridder {
     int max_batch = 1024;
     bool fused_fft = false;     // fft2_fused_ok(N, M): the 2-D FFT stages run as one kernel each
     int nstreams_fp = 2, nstreams_bp = 2;
-    int prec = kF32;
+    int prec = kF32;            // storage of the resident CAS volume the forward projection reads
+    int img_prec_set = -1;      // storage of the CAS images the back projection reads; -1: as prec
     int bp_mode = GG_BP_REF;
     bool five_taps = false;
     int ker_size = 501;
@@ -187,7 +188,8 @@ struct gg_gridder {
 
     Geom geom() const { return Geom{V, M, mask_radius, ker_size, ker_hw}; }
     const float *vol_scale() const { return prec == kF16 ? scales.p : nullptr; }
-    const float *img_scale() const { return prec == kF16 ? scales.p + 1 : nullptr; }
+    int img_prec() const { return img_prec_set < 0 ? prec : img_prec_set; }
+    const float *img_scale() const { return img_prec() == kF16 ? scales.p + 1 : nullptr; }
 };
 
 namespace {
@@ -234,7 +236,7 @@ void ensure_slot(gg_gridder *h, int s, int b, bool need_img)
     sl.real.ensure(MM * b);
     sl.spec.ensure(H * b);
     if (need_img) sl.img.ensure(NN * b);
-    if (h->prec != kF32) sl.casimg_lp.ensure(MM * b);
+    if (h->img_prec() != kF32) sl.casimg_lp.ensure(MM * b);
     if (!sl.ev_ready) GG_CK(cudaEventCreateWithFlags(&sl.ev_ready, cudaEventDisableTiming));
     if (!sl.ev_free) {
         GG_CK(cudaEventCreateWithFlags(&sl.ev_free, cudaEventDisableTiming));
@@ -390,29 +392,30 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
 {
     auto &S = h->slot[sl];
     const void *src = nullptr;
-    int iprec = h->prec;
+    const int ip = h->img_prec(); // storage of the CAS images read here
+    int iprec = ip;
     const float *scale = nullptr;
     if (!ones) {
         const size_t MM = (size_t)h->M * h->M;
         if (casimg) {
-            if (h->prec == kF32) {
+            if (ip == kF32) {
                 src = casimg;
             } else {
-                if (h->prec == kF16) GG_CK(launch_storage_scale(casimg, MM * b, 8192.0f, h->work.p, h->scales.p + 1, s));
-                GG_CK(launch_convert(casimg, S.casimg_lp.p, h->prec, MM * b, h->img_scale(), s));
+                if (ip == kF16) GG_CK(launch_storage_scale(casimg, MM * b, 8192.0f, h->work.p, h->scales.p + 1, s));
+                GG_CK(launch_convert(casimg, S.casimg_lp.p, ip, MM * b, h->img_scale(), s));
                 src = S.casimg_lp.p;
                 scale = h->img_scale();
             }
-        } else if (h->fused_fft && h->prec != kF16) {
-            void *dst = h->prec == kF32 ? (void *)S.casimg.p : (void *)S.casimg_lp.p;
-            GG_CK(launch_images_to_cas_fused(img, h->N, h->M, b, dst, h->prec, false, s));
+        } else if (h->fused_fft && ip != kF16) {
+            void *dst = ip == kF32 ? (void *)S.casimg.p : (void *)S.casimg_lp.p;
+            GG_CK(launch_images_to_cas_fused(img, h->N, h->M, b, dst, ip, false, s));
             src = dst;
         } else if (h->fused_fft) {
             // FP16: FP32 CAS images first, then the storage scale from their
             // largest magnitude and the conversion
             GG_CK(launch_images_to_cas_fused(img, h->N, h->M, b, S.casimg.p, kF32, false, s));
             GG_CK(launch_storage_scale(S.casimg.p, MM * b, 8192.0f, h->work.p, h->scales.p + 1, s));
-            GG_CK(launch_convert(S.casimg.p, S.casimg_lp.p, h->prec, MM * b, h->img_scale(), s));
+            GG_CK(launch_convert(S.casimg.p, S.casimg_lp.p, ip, MM * b, h->img_scale(), s));
             src = S.casimg_lp.p;
             scale = h->img_scale();
         } else {
@@ -420,12 +423,12 @@ void bp_batch(gg_gridder *h, const float *d_axes, int b, const float *img, const
             cufftHandle p = plan2d(h, CUFFT_R2C, b);
             GG_CKF(cufftSetStream(p, s));
             GG_CKF(cufftExecR2C(p, S.real.p, S.spec.p));
-            if (h->prec == kF16)
+            if (ip == kF16)
                 // |Re + Im| <= 2 max(|Re|, |Im|)
                 GG_CK(launch_storage_scale((const float *)S.spec.p, (size_t)h->M * (h->M / 2 + 1) * 2 * b, 4096.0f,
                                            h->work.p, h->scales.p + 1, s));
-            void *dst = h->prec == kF32 ? (void *)S.casimg.p : (void *)S.casimg_lp.p;
-            GG_CK(launch_spectrum_to_cas_images(S.spec.p, h->M, b, dst, h->prec, h->img_scale(), s));
+            void *dst = ip == kF32 ? (void *)S.casimg.p : (void *)S.casimg_lp.p;
+            GG_CK(launch_spectrum_to_cas_images(S.spec.p, h->M, b, dst, ip, h->img_scale(), s));
             src = dst;
             scale = h->img_scale();
         }
@@ -469,7 +472,7 @@ void ctf_batch(gg_gridder *h, const float *d_axes, int b, const float *img, cons
     }
     // CAS images *= CTF, and CTF^2 into S.real (free after the R2C), in one pass
     GG_CK(launch_ctf(S.casimg.p, 1, S.real.p, 2, h->M, b, d_defocus, d_defocus_v, d_astig, c, s));
-    if (h->prec == kF32 && h->bp_mode != GG_BP_ADJOINT) {
+    if (h->img_prec() == kF32 && h->bp_mode != GG_BP_ADJOINT) {
         // both stacks in one back-projection pass
         ProfScope ps(h, s, GG_KERNEL_BACK);
         GG_CK(launch_back_project_ref_pair(h->cas.p, h->pd.p, S.casimg.p, S.real.p, h->ker.p, d_axes, b, h->geom(), s));
@@ -896,6 +899,19 @@ extern "C" int gg_set_precision(gg_gridder *h, int precision)
             GG_CK(cudaStreamSynchronize(h->cs));
             h->prec = precision;
             h->cas_fp_valid = false;
+            for (auto &S : h->slot) S.casimg_lp.release();
+        }
+    });
+}
+
+extern "C" int gg_set_image_precision(gg_gridder *h, int precision)
+{
+    return guarded(h, [&] {
+        if (precision != -1 && precision != GG_PREC_F32 && precision != GG_PREC_F16 && precision != GG_PREC_BF16)
+            fail(GG_ERR_INVALID_ARG, "unknown image precision %d", precision);
+        if (precision != h->img_prec_set) {
+            GG_CK(cudaStreamSynchronize(h->cs));
+            h->img_prec_set = precision;
             for (auto &S : h->slot) S.casimg_lp.release();
         }
     });

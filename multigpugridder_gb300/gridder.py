@@ -133,6 +133,15 @@ class MultiGPUGridder:
     def set_precision(self, precision):
         self._call("gg_set_precision", _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision))
 
+    def set_image_precision(self, precision):
+        """Storage of the CAS images the back projection reads ("f32",
+        "bf16", "f16"), or None to follow set_precision (the default)."""
+        if precision is None:
+            code = -1
+        else:
+            code = _lib.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self._call("gg_set_image_precision", code)
+
     def set_bp_mode(self, mode):
         self._call("gg_set_bp_mode", _lib.BP_MODES[mode] if isinstance(mode, str) else int(mode))
 

@@ -81,3 +81,31 @@ def test_f16_scaling_handles_large_values(cuda, case):
         cas = g.getCASVolume()
     assert np.all(np.isfinite(imgs)) and np.all(np.isfinite(cas))
     assert O.rel_l2(imgs, imgs64 * 1e6) < TOL_REDUCED
+
+
+def test_image_precision_knob(cuda, case):
+    """BF16 volume with FP32 CAS images for the back projection
+    (gg_set_image_precision): the back projection equals the FP32 mode's bit
+    for bit (it does not read the volume), the forward projection equals the
+    BF16 mode's, and None restores the volume's precision for the images."""
+    import multigpugridder_gb300 as gg
+
+    N, p, vol, axes, imgs64, cas64 = case
+    imgs = imgs64.astype(np.float32)
+    with gg.MultiGPUGridder(N, len(axes), precision="f32", adjustInterpFactor=False) as g:
+        g.backProject(imgs, axes)
+        bp32 = g.getCASVolume()
+    with gg.MultiGPUGridder(N, len(axes), precision="bf16", adjustInterpFactor=False) as g:
+        g.setVolume(vol)
+        fp16b = g.forwardProject(axes)
+        g.backProject(imgs, axes)
+        bp16b = g.getCASVolume()
+    with gg.MultiGPUGridder(N, len(axes), precision="bf16", adjustInterpFactor=False) as g:
+        g.set_image_precision("f32")
+        g.setVolume(vol)
+        assert np.array_equal(g.forwardProject(axes), fp16b)
+        g.backProject(imgs, axes)
+        assert np.array_equal(g.getCASVolume(), bp32)
+        g.set_image_precision(None)
+        g.backProject(imgs, axes)
+        assert np.array_equal(g.getCASVolume(), bp16b)
