@@ -458,6 +458,34 @@ struct BpShape {
 // reads as zero), so the windows read them at constant offsets.
 constexpr int kTabRep = 1; // interleaved table copies
 
+// A 2-byte value held in the low 16 bits of u, widened to FP32 exactly.
+template <typename T> __device__ __forceinline__ float widen16(unsigned u);
+template <> __device__ __forceinline__ float widen16<__nv_bfloat16>(unsigned u) { return __uint_as_float(u << 16); }
+template <> __device__ __forceinline__ float widen16<__half>(unsigned u)
+{
+    return __half2float(__ushort_as_half((unsigned short)u));
+}
+template <> __device__ __forceinline__ float widen16<float>(unsigned u) { return __uint_as_float(u); }
+
+// Four consecutive values from a 4-element-aligned address, as FP32.
+__device__ __forceinline__ void ld_quad(const float *p, float (&v)[4])
+{
+    const float4 q = __ldg(reinterpret_cast<const float4 *>(p));
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+}
+template <typename T>
+__device__ __forceinline__ void ld_quad(const T *p, float (&v)[4])
+{
+    const uint2 w = __ldg(reinterpret_cast<const uint2 *>(p));
+    v[0] = widen16<T>(w.x & 0xffffu);
+    v[1] = widen16<T>(w.x >> 16);
+    v[2] = widen16<T>(w.y & 0xffffu);
+    v[3] = widen16<T>(w.y >> 16);
+}
+
 __device__ __forceinline__ float lds_f32(unsigned addr)
 {
     float v;
@@ -624,7 +652,7 @@ __global__ void __launch_bounds__(kCThreads, 3)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
                       float kerHW, int bricksX, int bricksY, int tabPad, int zeroEdges,
-                      const float *__restrict__ d_scale, const float *__restrict__ img2)
+                      const float *__restrict__ d_scale, const float *__restrict__ img2, int vecImg)
 {
     static_assert(!DW || (!ONES && !DENS && !ADJ), "the second image stack is a reference-rule option");
     constexpr int W = ADJ ? 7 : 5, HALF = W / 2;
@@ -802,7 +830,57 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 const int fw = (int)floorf(ic + hi + 0.6f) + HALF - fi0 + 1;
                 fh = (int)floorf(jc + hj + 0.6f) + HALF - fj0 + 1;
                 foot = fw <= FW && fh <= FH && fh >= W && (!ADJ || zeroEdges);
-                if (foot && !ADJ) {
+                if (foot && !ADJ && !ONES && vecImg) {
+                    // vector loads of aligned pixel quads (rows start at
+                    // multiples of 4 elements: 4 divides M, the image stacks
+                    // are aligned), the linear-index rule still applied
+                    // pixel by pixel
+                    constexpr int NQ = FW / 4 + 1; // quads per footprint row
+                    const int base = fi0 & ~3, sh = fi0 & 3;
+                    for (int t = lane; t < fh * NQ; t += 32) {
+                        const int r = t / NQ, qq = t - r * NQ;
+                        const int c0 = 4 * qq - sh; // footprint column of the quad's first pixel
+                        const int lin0 = (fj0 + r) * M + base + 4 * qq;
+                        float v[4] = {0.0f, 0.0f, 0.0f, 0.0f}, v2[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+                        if (lin0 >= 0 && lin0 + 3 < MM) {
+                            ld_quad(img_ptr + lin0, v);
+                            if (DW) ld_quad(img2_ptr + lin0, v2);
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < 4; e++)
+                                if (lin0 + e >= 0 && lin0 + e < MM) {
+                                    v[e] = ld_f32(img_ptr + lin0 + e);
+                                    if (DW) v2[e] = __ldg(img2_ptr + lin0 + e);
+                                }
+                        }
+#pragma unroll
+                        for (int e = 0; e < 4; e++)
+                            if (c0 + e >= 0 && c0 + e < FW) {
+                                wfoot[r * FS + c0 + e] = v[e];
+                                if (DW) wfoot2[r * FS + c0 + e] = v2[e];
+                            }
+                    }
+                } else if (foot && !ADJ && sizeof(TI) == 2 && !ONES && !(M & 1)) {
+                    // the same with 4-byte pixel pairs when only 2 divides M
+                    constexpr int NPR = FW / 2 + 1; // pairs per footprint row
+                    const int base = fi0 & ~1, odd = fi0 & 1;
+                    for (int t = lane; t < fh * NPR; t += 32) {
+                        const int r = t / NPR, pp = t - r * NPR;
+                        const int c0 = 2 * pp - odd; // footprint column of the pair's first pixel
+                        const int lin0 = (fj0 + r) * M + base + 2 * pp;
+                        float v0 = 0.0f, v1 = 0.0f;
+                        if (lin0 >= 0 && lin0 + 1 < MM) {
+                            const unsigned w = __ldg(reinterpret_cast<const unsigned *>(img_ptr + lin0));
+                            v0 = widen16<TI>(w & 0xffffu);
+                            v1 = widen16<TI>(w >> 16);
+                        } else {
+                            if (lin0 >= 0 && lin0 < MM) v0 = ld_f32(img_ptr + lin0);
+                            if (lin0 + 1 >= 0 && lin0 + 1 < MM) v1 = ld_f32(img_ptr + lin0 + 1);
+                        }
+                        if (c0 >= 0 && c0 < FW) wfoot[r * FS + c0] = v0;
+                        if (c0 + 1 < FW) wfoot[r * FS + c0 + 1] = v1; // c0 + 1 >= 0
+                    }
+                } else if (foot && !ADJ) {
                     // the reference's linear-index rule (gpuBackProject.cu:99)
                     for (int t = lane; t < fh * FW; t += 32) {
                         const int r = t / FW, c = t - r * FW;
@@ -899,8 +977,11 @@ static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *k
     auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
+    // quad loads of image rows: 4 | M and the stacks aligned to 4 elements
+    const size_t qa = 4 * sizeof(TI);
+    const int vec = (g.M % 4 == 0) && ((size_t)img % qa == 0) && (!img2 || (size_t)img2 % 16 == 0) ? 1 : 0;
     kern<<<(unsigned)nb, kCThreads, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
-                                              g.ker_hw, bx, by, pad, zero_edges ? 1 : 0, scale, img2);
+                                              g.ker_hw, bx, by, pad, zero_edges ? 1 : 0, scale, img2, vec);
     count_launches(1);
     return cudaGetLastError();
 }
