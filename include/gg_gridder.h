@@ -89,11 +89,9 @@ int gg_set_num_streams_fp(gg_gridder *h, int n);                    /* SetNumStr
 int gg_set_num_streams_bp(gg_gridder *h, int n);                    /* SetNumStreamsBP */
 int gg_set_precision(gg_gridder *h, int precision);                 /* GG_PREC_*: storage of CAS volume / CAS images */
 /* Storage of the CAS images the back projection reads, apart from the CAS
-   volume's: GG_PREC_* or -1 (the default) to follow gg_set_precision.  The
-   back projection is not bandwidth-bound, and with 2-byte images it measured
-   5-9% slower, so a BF16/FP16 volume with FP32 images
-   (gg_set_image_precision(h, GG_PREC_F32)) is the fastest reduced-precision
-   setting.  No counterpart in the reference. */
+   volume's: GG_PREC_* or -1 (the default) to follow gg_set_precision.
+   GG_PREC_F32 under a 2-byte volume keeps the images exact; it costs about
+   the same as 2-byte images.  No counterpart in the reference. */
 int gg_set_image_precision(gg_gridder *h, int precision);
 int gg_set_bp_mode(gg_gridder *h, int mode);                        /* GG_BP_REF (default) or GG_BP_ADJOINT */
 
