@@ -9,6 +9,7 @@
 // centre M/2, nearest-index lookup into the KB table, int mask radius.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "gg_common.cuh"
 #include "gg_internal.h"
@@ -42,10 +43,12 @@ __device__ __forceinline__ float voxel_proj(float a0, float a1, float a2, float 
 // kerCenter + 1/2)): equal for every float r in [-2, 2] (checked
 // exhaustively) and one conversion instead of a roundf and a conversion.
 // Callers pass r in [-2, 2]; the clamp only keeps a NaN or infinite
-// coordinate (bad axes) inside the table.
-__device__ __forceinline__ float kb_weight(const float *sker, float r, float kerScale, float kerCenterHalf, int kerSize)
+// coordinate (bad axes) inside the table.  Entry k is read at sker[k * rep]
+// (rep interleaved copies).
+__device__ __forceinline__ float kb_weight(const float *sker, float r, float kerScale, float kerCenterHalf, int kerSize,
+                                           int rep = 1)
 {
-    return sker[min(max(__float2int_rd(__fmaf_rn(r, kerScale, kerCenterHalf)), 0), kerSize - 1)];
+    return sker[min(max(__float2int_rd(__fmaf_rn(r, kerScale, kerCenterHalf)), 0), kerSize - 1) * rep];
 }
 
 __device__ __forceinline__ void load_table(float *sker, const float *ker, int kerSize)
@@ -374,12 +377,12 @@ __device__ __forceinline__ float ref_pixel_pos(float pi, float pj, float n_x, fl
 // the reference's roundf(fma(r, kerScale, kerCenter)) for every float r in
 // [-2, 2] (checked exhaustively): both round the same exact value once.
 // INSIDE: the whole window lies in the image, so the reference's
-// linear-index test always passes.  Table entry k is read at sker[k * REP].
+// linear-index test always passes.  Table entry k is read at sker[k * rep].
 // DW: cumW sums img2 * w (a second image back-projected in the same pass,
 // fused as cumSum is) instead of w.
-template <typename TI, bool ONES, bool DENS, bool INSIDE, int REP = 1, bool DW = false>
-__device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker, const TI *__restrict__ img_ptr, int M,
-                                           int imgi, int imgj, int imgCenter, float &cumSum, float &cumW,
+template <typename TI, bool ONES, bool DENS, bool INSIDE, bool DW = false>
+__device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker, int rep, const TI *__restrict__ img_ptr,
+                                           int M, int imgi, int imgj, int imgCenter, float &cumSum, float &cumW,
                                            const float *__restrict__ img2_ptr = nullptr)
 {
 #pragma unroll
@@ -391,11 +394,11 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
             const int i1 = imgi + io;
             const float pi = (float)(i1 - imgCenter);
             float r = fminf(fmaxf(ref_pixel_pos(pi, pj, q.nx0, q.ny0, q.vc) - q.vi, -2.0f), 2.0f);
-            float w = sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf)) * REP];
+            float w = sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf)) * rep];
             r = fminf(fmaxf(ref_pixel_pos(pi, pj, q.nx1, q.ny1, q.vc) - q.vj, -2.0f), 2.0f);
-            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf)) * REP]);
+            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf)) * rep]);
             r = fminf(fmaxf(ref_pixel_pos(pi, pj, q.nx2, q.ny2, q.vc) - q.vk, -2.0f), 2.0f);
-            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf)) * REP]);
+            w = __fmul_rn(w, sker[__float2int_rd(__fmaf_rn(r, q.kerScale, q.kerCenterHalf)) * rep]);
             const int lin = j1 * M + i1;
             if (INSIDE || (lin < M * M && lin >= 0)) {
                 // cumSum += img * w, fused as the reference's build fuses it
@@ -411,15 +414,19 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
 // Back projection, reference window rule
 // ---------------------------------------------------------------------------
 // Only the voxels inside a direction's slab (|f_imgk| <= 2, a few percent of
-// the volume) run the 25-pixel window.  A CTA owns a 16x8x(2 BD) brick and
-// each warp an 8x4xBD block of it, BD voxels per lane: block voxel
-// l = lane + 32 s (x = l & 7, y = (l >> 3) & 3, z = l >> 5).  Per direction a
-// warp tests its 32 BD voxels against the slab, lists the active ones in shared memory and
-// runs them 32 at a time, one per lane.  Every voxel still receives its
-// directions one by one in order and its window in the reference's order, so
-// the per-voxel sums are those of the reference kernel's loops, bit for bit.
+// the volume) run the 25-pixel window.  A group of 256 threads (8 warps) owns
+// a 16x8x(2 BD) brick and each warp an 8x4xBD block of it, BD voxels per lane:
+// block voxel l = lane + 32 s (x = l & 7, y = (l >> 3) & 3, z = l >> 5).  Per
+// direction a warp tests its 32 BD voxels against the slab, lists the active
+// ones in shared memory and runs them 32 at a time, one per lane.  Every voxel
+// still receives its directions one by one in order and its window in the
+// reference's order, so the per-voxel sums are those of the reference
+// kernel's loops, bit for bit.  A CTA holds kBpGroups groups on neighbouring
+// bricks, which share one copy of the KB table (below); each group
+// synchronises on its own named barrier.
 constexpr int kCBX = 16, kCBY = 8; // brick: 2x2x2 warp blocks of 8x4xBD (BD = 8, or 4 for ADJ / DW)
-constexpr int kCThreads = 256;
+constexpr int kCThreads = 256;  // threads of a group
+constexpr int kBpGroups = 3;    // groups (bricks) per CTA, one CTA per SM
 static_assert(kBpChunk % kCThreads == 0, "the cull gives each thread kBpChunk / kCThreads directions");
 // Depth of a warp block for the reference rule: 6 voxels, or 8 (DEEP) on CAS
 // images of 512^2 and more.  Deeper blocks have more active voxels per
@@ -445,18 +452,33 @@ struct BpShape {
 // h = kerCenter + 1/2 (see kb_weight).  For v >= 4 and |Q - v| <= 2,
 // Sterbenz's lemma makes fl(Q - v) = Q - v exact, so that fma and
 // fma(Q, s, h - v*s) round the same real number (h - v*s is exact: s and h
-// are multiples of 1/4); for |Q - v| > 2 both land beyond the same end of the
-// table, where a padded table repeating the edge entries stands in for the
-// clamp.  floor(x) for |x| < 2^22 is the low bits of x + 1.5*2^23 added with
-// round-down.  Checked on the CPU against the reference formula for every
-// float Q within 4.2 of v (v = 4..40; tables of 501 and 1000 entries) and on
-// random samples up to v = 600: identical indices.
+// are multiples of 1/4).  Scaled by 1/P, P a power of two >= kerSize - 1,
+// y = fma(Q, s/P, (h - v*s)/P) is that rounded value over P exactly, and the
+// saturating fma clamps it to [0, 1]: for |Q - v| > 2 it lands at or beyond
+// the same end of the table as the reference's clamp, and a table of P + 1
+// entries that repeats the last one past kerSize - 1 gives the clamped
+// entry.  floor(P y) is the low bits of y + 1.5*2^23/P added with round-down.
+// Checked on the CPU against the reference formula for every float Q within
+// 4.2 of v (v = 4..40; tables of 501 and 1000 entries) and on random samples
+// up to v = 600: identical entries.
+//
+// The table is held in `copies` interleaved copies (entry k of copy c at word
+// k * copies + c) and lane l reads copy l % copies.  With 32 copies (66 KB
+// for P = 512) each lane reads its own bank, so the three data-dependent
+// lookups per pixel never conflict; shared by the groups of a CTA, the table
+// fits beside their working sets.
 //
 // The pixels come from a per-warp footprint in shared memory: the pixels any
 // window of the warp's block can touch, staged per direction with the
 // reference's linear-index rule (a pixel whose index falls outside the image
 // reads as zero), so the windows read them at constant offsets.
-constexpr int kTabRep = 1; // interleaved table copies
+struct BpTable {
+    int copies;          // interleaved copies (32: conflict-free)
+    int entries;         // P + 1
+    float scale;         // 1 / P
+    float magic;         // 1.5 * 2^23 / P
+    unsigned magic_bits; // its bits: entry floor(P y) sits at bits(y + magic) - magic_bits
+};
 
 // A 2-byte value held in the low 16 bits of u, widened to FP32 exactly.
 template <typename T> __device__ __forceinline__ float widen16(unsigned u);
@@ -496,13 +518,23 @@ __device__ __forceinline__ float lds_f32(unsigned addr)
 struct FootWin {
     float nx0, nx1, nx2, ny0, ny1, ny2;
     float vc;         // volume centre
-    float s;          // kerScale
-    float c0, c1, c2; // h - v*s per axis
+    float s;          // kerScale / P
+    float c0, c1, c2; // (h - v*s) / P per axis
+    float mg;         // 1.5 * 2^23 / P
+    unsigned stride;  // bytes between table entries
 };
 
+// fma rounded to nearest, clamped to [0, 1] (a NaN gives 0).
+__device__ __forceinline__ float fma_sat(float a, float b, float c)
+{
+    float d;
+    asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // One voxel's WI x WJ window from the footprint (fbase = its top-left pixel,
-// rows FS apart); table entry floor(x) is read at
-// tab + bits(x + 1.5*2^23) * 4 * kTabRep.  Sums row by row, as the reference.
+// rows FS apart); table entry floor(P y) is read at
+// tab + bits(y + q.mg) * q.stride.  Sums row by row, as the reference.
 template <bool DENS, int WI, int WJ, int FS, bool DW = false>
 __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase, unsigned tab, float pi0, float pj0,
                                             float &cumSum, float &cumW, const float *fbase2 = nullptr)
@@ -517,12 +549,12 @@ __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase
             const float q0 = __fadd_rn(__fmaf_rn(pi, q.nx0, py0), q.vc);
             const float q1 = __fadd_rn(__fmaf_rn(pi, q.nx1, py1), q.vc);
             const float q2 = __fadd_rn(__fmaf_rn(pi, q.nx2, py2), q.vc);
-            const unsigned b0 = __float_as_uint(__fadd_rd(__fmaf_rn(q0, q.s, q.c0), 12582912.0f));
-            const unsigned b1 = __float_as_uint(__fadd_rd(__fmaf_rn(q1, q.s, q.c1), 12582912.0f));
-            const unsigned b2 = __float_as_uint(__fadd_rd(__fmaf_rn(q2, q.s, q.c2), 12582912.0f));
-            float w = lds_f32(tab + b0 * (4u * kTabRep));
-            w = __fmul_rn(w, lds_f32(tab + b1 * (4u * kTabRep)));
-            w = __fmul_rn(w, lds_f32(tab + b2 * (4u * kTabRep)));
+            const unsigned b0 = __float_as_uint(__fadd_rd(fma_sat(q0, q.s, q.c0), q.mg));
+            const unsigned b1 = __float_as_uint(__fadd_rd(fma_sat(q1, q.s, q.c1), q.mg));
+            const unsigned b2 = __float_as_uint(__fadd_rd(fma_sat(q2, q.s, q.c2), q.mg));
+            float w = lds_f32(tab + b0 * q.stride);
+            w = __fmul_rn(w, lds_f32(tab + b1 * q.stride));
+            w = __fmul_rn(w, lds_f32(tab + b2 * q.stride));
             cumSum = __fmaf_rn(fbase[jo * FS + io], w, cumSum);
             if (DENS) cumW = __fadd_rn(cumW, w);
             if (DW) cumW = __fmaf_rn(fbase2[jo * FS + io], w, cumW);
@@ -531,11 +563,11 @@ __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase
 }
 
 // foot_window with adjacent pixels of a row taken in pairs by the packed
-// FP32x2 instructions (sm_100+): the pixel positions, the table indices and
-// the weight products of two pixels per instruction.  Each lane of a packed
-// instruction rounds as the scalar instruction does, so every weight, and
-// every sum (accumulated one pixel at a time in the same order), is
-// bit-identical to foot_window's.
+// FP32x2 instructions (sm_100+): the pixel positions, the table addresses and
+// the weight products of two pixels per instruction (the saturating index fma
+// has no packed form).  Each lane of a packed instruction rounds as the scalar
+// instruction does, so every weight, and every sum (accumulated one pixel at a
+// time in the same order), is bit-identical to foot_window's.
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
 template <bool DENS, int WI, int WJ, int FS, bool DW = false>
@@ -543,8 +575,7 @@ __device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fb
                                                float pj0, float &cumSum, float &cumW, const float *fbase2 = nullptr)
 {
     const float2 nx0 = f2(q.nx0, q.nx0), nx1 = f2(q.nx1, q.nx1), nx2 = f2(q.nx2, q.nx2);
-    const float2 vc = f2(q.vc, q.vc), sc = f2(q.s, q.s), mg = f2(12582912.0f, 12582912.0f);
-    const float2 c0 = f2(q.c0, q.c0), c1 = f2(q.c1, q.c1), c2 = f2(q.c2, q.c2);
+    const float2 vc = f2(q.vc, q.vc), mg = f2(q.mg, q.mg);
 #pragma unroll
     for (int jo = 0; jo < WJ; jo++) {
         const float pj = pj0 + (float)jo;
@@ -556,15 +587,15 @@ __device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fb
             const float2 q0 = __fadd2_rn(__ffma2_rn(pi, nx0, qy0), vc);
             const float2 q1 = __fadd2_rn(__ffma2_rn(pi, nx1, qy1), vc);
             const float2 q2 = __fadd2_rn(__ffma2_rn(pi, nx2, qy2), vc);
-            const float2 b0 = __fadd2_rd(__ffma2_rn(q0, sc, c0), mg);
-            const float2 b1 = __fadd2_rd(__ffma2_rn(q1, sc, c1), mg);
-            const float2 b2 = __fadd2_rd(__ffma2_rn(q2, sc, c2), mg);
-            const float2 t0 = f2(lds_f32(tab + __float_as_uint(b0.x) * (4u * kTabRep)),
-                                 lds_f32(tab + __float_as_uint(b0.y) * (4u * kTabRep)));
-            const float2 t1 = f2(lds_f32(tab + __float_as_uint(b1.x) * (4u * kTabRep)),
-                                 lds_f32(tab + __float_as_uint(b1.y) * (4u * kTabRep)));
-            const float2 t2 = f2(lds_f32(tab + __float_as_uint(b2.x) * (4u * kTabRep)),
-                                 lds_f32(tab + __float_as_uint(b2.y) * (4u * kTabRep)));
+            const float2 b0 = __fadd2_rd(f2(fma_sat(q0.x, q.s, q.c0), fma_sat(q0.y, q.s, q.c0)), mg);
+            const float2 b1 = __fadd2_rd(f2(fma_sat(q1.x, q.s, q.c1), fma_sat(q1.y, q.s, q.c1)), mg);
+            const float2 b2 = __fadd2_rd(f2(fma_sat(q2.x, q.s, q.c2), fma_sat(q2.y, q.s, q.c2)), mg);
+            const float2 t0 = f2(lds_f32(tab + __float_as_uint(b0.x) * q.stride),
+                                 lds_f32(tab + __float_as_uint(b0.y) * q.stride));
+            const float2 t1 = f2(lds_f32(tab + __float_as_uint(b1.x) * q.stride),
+                                 lds_f32(tab + __float_as_uint(b1.y) * q.stride));
+            const float2 t2 = f2(lds_f32(tab + __float_as_uint(b2.x) * q.stride),
+                                 lds_f32(tab + __float_as_uint(b2.y) * q.stride));
             const float2 w = __fmul2_rn(__fmul2_rn(t0, t1), t2);
             cumSum = __fmaf_rn(fbase[jo * FS + io], w.x, cumSum);
             if (DENS) cumW = __fadd_rn(cumW, w.x);
@@ -579,12 +610,12 @@ __device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fb
             const float q0 = __fadd_rn(__fmaf_rn(pi, q.nx0, py0), q.vc);
             const float q1 = __fadd_rn(__fmaf_rn(pi, q.nx1, py1), q.vc);
             const float q2 = __fadd_rn(__fmaf_rn(pi, q.nx2, py2), q.vc);
-            const unsigned b0 = __float_as_uint(__fadd_rd(__fmaf_rn(q0, q.s, q.c0), 12582912.0f));
-            const unsigned b1 = __float_as_uint(__fadd_rd(__fmaf_rn(q1, q.s, q.c1), 12582912.0f));
-            const unsigned b2 = __float_as_uint(__fadd_rd(__fmaf_rn(q2, q.s, q.c2), 12582912.0f));
-            float w = lds_f32(tab + b0 * (4u * kTabRep));
-            w = __fmul_rn(w, lds_f32(tab + b1 * (4u * kTabRep)));
-            w = __fmul_rn(w, lds_f32(tab + b2 * (4u * kTabRep)));
+            const unsigned b0 = __float_as_uint(__fadd_rd(fma_sat(q0, q.s, q.c0), q.mg));
+            const unsigned b1 = __float_as_uint(__fadd_rd(fma_sat(q1, q.s, q.c1), q.mg));
+            const unsigned b2 = __float_as_uint(__fadd_rd(fma_sat(q2, q.s, q.c2), q.mg));
+            float w = lds_f32(tab + b0 * q.stride);
+            w = __fmul_rn(w, lds_f32(tab + b1 * q.stride));
+            w = __fmul_rn(w, lds_f32(tab + b2 * q.stride));
             cumSum = __fmaf_rn(fbase[jo * FS + io], w, cumSum);
             if (DENS) cumW = __fadd_rn(cumW, w);
             if (DW) cumW = __fmaf_rn(fbase2[jo * FS + io], w, cumW);
@@ -592,12 +623,34 @@ __device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fb
     }
 }
 
-// Table entries below and above the table a window can reach with
-// orthonormal axes: |Q - v| <= sqrt(2.5^2 + 2.5^2 + 2^2) < 4.1 per axis for
-// the reference window, sqrt(3.5^2 + 3.5^2 + 3.47^2) < 6.1 for the adjoint's.
-static inline int bp_table_pad(int kerSize, bool adj)
+static int max_dyn_smem()
 {
-    return (int)ceil((adj ? 6.25 : 4.25) * (kerSize - 1) / 4.0) + 2;
+    static int bytes = 0;
+    if (bytes == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&bytes, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (bytes <= 0) bytes = 48 * 1024;
+    }
+    return bytes;
+}
+
+// The table layout for kerSize entries beside kBpGroups working sets of
+// group_bytes: P = 512 (kerSize <= 513) or the next power of two, and as many
+// copies, 32 down to 1, as fit.  copies = 0: not even one copy fits.
+static BpTable bp_table(int kerSize, size_t group_bytes)
+{
+    int P = 512;
+    while (P < kerSize - 1) P *= 2;
+    BpTable t;
+    t.entries = P + 1;
+    t.scale = 1.0f / (float)P;
+    t.magic = 12582912.0f / (float)P;
+    std::memcpy(&t.magic_bits, &t.magic, sizeof(float));
+    t.copies = 32;
+    const size_t limit = (size_t)max_dyn_smem();
+    while (t.copies > 0 && (size_t)t.entries * t.copies * sizeof(float) + kBpGroups * group_bytes > limit) t.copies /= 2;
+    return t;
 }
 
 // The exact adjoint of fp_kernel<., 4> for one voxel, without the fast
@@ -607,7 +660,8 @@ static inline int bp_table_pad(int kerSize, bool adj)
 template <typename TI>
 __device__ float adjoint_window_slow(int vi, int vj, int vk, int volCenter, float nx0, float nx1, float nx2, float ny0,
                                      float ny1, float ny2, const TI *__restrict__ img_ptr, int M, int imgCenter,
-                                     int maskR, const float *sker, float kerScale, float kerCenterHalf, int kerSize)
+                                     int maskR, const float *sker, int rep, float kerScale, float kerCenterHalf,
+                                     int kerSize)
 {
     const float pi = ((float)vi - volCenter) * nx0 + ((float)vj - volCenter) * nx1 + ((float)vk - volCenter) * nx2;
     const float pj = ((float)vi - volCenter) * ny0 + ((float)vj - volCenter) * ny1 + ((float)vk - volCenter) * ny2;
@@ -626,9 +680,9 @@ __device__ float adjoint_window_slow(int vi, int vj, int vk, int volCenter, floa
             // membership in the forward window floor(f)-1 .. floor(f)+2
             const int oi = vi - ((int)floorf(fi) - 1), oj = vj - ((int)floorf(fj) - 1), ok = vk - ((int)floorf(fk) - 1);
             if ((unsigned)oi > 3u || (unsigned)oj > 3u || (unsigned)ok > 3u) continue;
-            const float w = kb_weight(sker, (float)vi - fi, kerScale, kerCenterHalf, kerSize) *
-                            kb_weight(sker, (float)vj - fj, kerScale, kerCenterHalf, kerSize) *
-                            kb_weight(sker, (float)vk - fk, kerScale, kerCenterHalf, kerSize);
+            const float w = kb_weight(sker, (float)vi - fi, kerScale, kerCenterHalf, kerSize, rep) *
+                            kb_weight(sker, (float)vj - fj, kerScale, kerCenterHalf, kerSize, rep) *
+                            kb_weight(sker, (float)vk - fk, kerScale, kerCenterHalf, kerSize, rep);
             s = fmaf(w, ld_f32(img_ptr + (size_t)pxj * M + pxi), s);
         }
     }
@@ -647,11 +701,34 @@ __device__ float adjoint_window_slow(int vi, int vj, int vk, int volCenter, floa
 // DW (reference rule, FP32 images): pd accumulates the back projection of a
 // second image stack img2 (the same directions) in the same pass, with the
 // same weights and summation order as a separate back projection of img2.
+// One group's working set in shared memory (after the table).
+template <bool DENS, bool ADJ, bool DW, bool DEEP>
+struct BpGroupMem {
+    using Shape = BpShape<ADJ, DW, DEEP>;
+    static constexpr int NW = kCThreads / 32, WV = Shape::WV, FP = Shape::FW * (Shape::FW + 1);
+    float sax[kBpChunk * 9];
+    int slist[kBpChunk];
+    int swarp[kBpChunk / 32]; // kept directions per (pass, warp)
+    int scount;
+    // per-voxel sums [warp][block voxel]; a voxel is updated by at most one
+    // lane per direction, directions in order, so no atomics are needed
+    float sacc[NW * WV];
+    float saccw[DENS || DW ? NW * WV : 1];
+    float sfoot[NW * FP];
+    float sfoot2[DW ? NW * FP : 1];
+    unsigned char svox[NW * WV];
+};
+
+__device__ __forceinline__ void group_sync(int id)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(kCThreads) : "memory");
+}
+
 template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false, bool DEEP = false>
-__global__ void __launch_bounds__(kCThreads, 3)
+__global__ void __launch_bounds__(kCThreads *kBpGroups, 1)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
-                      float kerHW, int bricksX, int bricksY, int tabPad, int zeroEdges,
+                      float kerHW, int bricksX, int bricksY, int nBricks, BpTable tb, int zeroEdges,
                       const float *__restrict__ d_scale, const float *__restrict__ img2, int vecImg)
 {
     static_assert(!DW || (!ONES && !DENS && !ADJ), "the second image stack is a reference-rule option");
@@ -659,23 +736,22 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     using Shape = BpShape<ADJ, DW, DEEP>;
     constexpr int BD = Shape::BD, kWarpVox = Shape::WV, kCBZ = Shape::BZ;
     constexpr int FW = Shape::FW, FH = FW, FS = FW + 1;
-    extern __shared__ float stab[]; // (kerSize + 2 tabPad) entries x kTabRep copies
-    __shared__ float sax[kBpChunk * 9];
-    __shared__ int slist[kBpChunk];
-    __shared__ int swarp[kBpChunk / 32]; // kept directions per (pass, warp)
-    __shared__ int scount;
-    // per-voxel sums [warp][block voxel]; a voxel is updated by at most one
-    // lane per direction, directions in order, so no atomics are needed
-    __shared__ float sacc[kCThreads / 32 * kWarpVox];
-    __shared__ float saccw[DENS || DW ? kCThreads / 32 * kWarpVox : 1];
-    __shared__ float sfoot[kCThreads / 32 * FH * FS];
-    __shared__ float sfoot2[DW ? kCThreads / 32 * FH * FS : 1];
-    __shared__ unsigned char svox[kCThreads / 32 * kWarpVox];
+    using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
+    // [table: tb.entries x tb.copies][kBpGroups x Mem]
+    extern __shared__ __align__(16) float bp_smem[];
+    const int cp = tb.copies, tabWords = tb.entries * cp;
+    for (int t = threadIdx.x; t < tabWords; t += blockDim.x) bp_smem[t] = __ldg(ker + min(t / cp, kerSize - 1));
+    __syncthreads();
 
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int x0 = (blockIdx.x % bricksX) * kCBX;
-    const int y0 = ((blockIdx.x / bricksX) % bricksY) * kCBY;
-    const int z0 = (blockIdx.x / (bricksX * bricksY)) * kCBZ;
+    const int grp = threadIdx.x / kCThreads, brick = blockIdx.x * kBpGroups + grp;
+    if (brick >= nBricks) return;
+    Mem &sm = reinterpret_cast<Mem *>(bp_smem + tabWords)[grp];
+    float *sax = sm.sax;
+    int *slist = sm.slist, *swarp = sm.swarp;
+    const int tid = threadIdx.x - grp * kCThreads, warp = tid >> 5, lane = tid & 31;
+    const int x0 = (brick % bricksX) * kCBX;
+    const int y0 = ((brick / bricksX) % bricksY) * kCBY;
+    const int z0 = (brick / (bricksX * bricksY)) * kCBZ;
     const int bx = x0 + (warp & 1) * 8, by = y0 + ((warp >> 1) & 1) * 4, bz = z0 + (warp >> 2) * BD;
     const int volCenter = (int)((float)V) / 2;
     const int imgCenter = (int)((float)M) / 2;
@@ -688,11 +764,11 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         const float reach = ADJ ? (float)maskR + 4.0f : (float)maskR;
         if (cx * cx + cy * cy + cz * cz > reach * reach + 1.0f) return;
     }
-    for (int t = tid; t < (kerSize + 2 * tabPad) * kTabRep; t += kCThreads)
-        stab[t] = __ldg(ker + min(max(t / kTabRep - tabPad, 0), kerSize - 1));
-    const float *sker = stab + tabPad * kTabRep + lane % kTabRep; // entry k at sker[k * kTabRep]
-    const unsigned tab = (unsigned)__cvta_generic_to_shared(stab) + 4u * (unsigned)(lane % kTabRep) +
-                         4u * kTabRep * ((unsigned)tabPad - 0x4B400000u);
+    const float *sker = bp_smem + lane % cp; // entry k at sker[k * cp]
+    const unsigned stride = 4u * (unsigned)cp;
+    const unsigned tab = (unsigned)__cvta_generic_to_shared(bp_smem) + 4u * (unsigned)(lane % cp) - tb.magic_bits * stride;
+    float *sfoot = sm.sfoot, *sfoot2 = sm.sfoot2, *sacc = sm.sacc, *saccw = sm.saccw;
+    unsigned char *svox = sm.svox;
     float *wfoot = sfoot + warp * (FH * FS);
     float *wfoot2 = sfoot2 + (DW ? warp * (FH * FS) : 0);
     unsigned char *wvox = svox + warp * kWarpVox;
@@ -729,9 +805,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     const unsigned lt_mask = (1u << lane) - 1u;
     for (int c0 = 0; c0 < n; c0 += kBpChunk) {
         const int cn = min(kBpChunk, n - c0);
-        __syncthreads();
+        group_sync(grp + 1);
         for (int t = tid; t < cn * 9; t += kCThreads) sax[t] = __ldg(axes + (size_t)c0 * 9 + t);
-        __syncthreads();
+        group_sync(grp + 1);
         // cull: thread tid takes directions tid + p * kCThreads; the kept
         // ones are listed in direction order (pass by pass, warp by warp)
         constexpr int kPasses = kBpChunk / kCThreads;
@@ -765,7 +841,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             ballots[pss] = __ballot_sync(0xffffffffu, keep);
             if (lane == 0) swarp[pss * (kCThreads / 32) + warp] = __popc(ballots[pss]);
         }
-        __syncthreads();
+        group_sync(grp + 1);
         {
             int off = 0;
 #pragma unroll
@@ -775,10 +851,10 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 if (keeps[pss]) slist[o + __popc(ballots[pss] & lt_mask)] = (tid + pss * kCThreads) | orthos[pss];
                 for (int w = 0; w < kCThreads / 32; w++) off += swarp[pss * (kCThreads / 32) + w];
             }
-            if (tid == kCThreads - 1) scount = off;
+            if (tid == kCThreads - 1) sm.scount = off;
         }
-        __syncthreads();
-        const int count = scount;
+        group_sync(grp + 1);
+        const int count = sm.scount;
 
         for (int q = 0; q < count; q++) {
             const int e = slist[q];
@@ -924,25 +1000,27 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                         vi >= 4 && vj >= 4 && vk >= 4 && (ADJ || inside || !DENS)) {
                         // reference rule: index of r = Q - v; adjoint: of r = v - Q
                         const float sg = ADJ ? -kerScale : kerScale;
-                        const FootWin fwin{nx0, nx1, nx2, ny0, ny1, ny2, (float)volCenter, sg,
-                                           kerCenterHalf - (float)vi * sg, kerCenterHalf - (float)vj * sg,
-                                           kerCenterHalf - (float)vk * sg};
+                        // scaled by 1/P (exact): the saturating index form
+                        const FootWin fwin{nx0, nx1, nx2, ny0, ny1, ny2, (float)volCenter, sg * tb.scale,
+                                           (kerCenterHalf - (float)vi * sg) * tb.scale,
+                                           (kerCenterHalf - (float)vj * sg) * tb.scale,
+                                           (kerCenterHalf - (float)vk * sg) * tb.scale, tb.magic, stride};
                         const float *fb = wfoot + rj * FS + ri;
                         const float pi0 = (float)(imgi - HALF - imgCenter), pj0 = (float)(imgj - HALF - imgCenter);
                         foot_window_x2<DENS, W, W, FS, DW>(fwin, fb, tab, pi0, pj0, cs, cw,
                                                         DW ? wfoot2 + rj * FS + ri : nullptr);
                     } else if (ADJ) {
                         cs = adjoint_window_slow<TI>(vi, vj, vk, volCenter, nx0, nx1, nx2, ny0, ny1, ny2, img_ptr, M,
-                                                     imgCenter, maskR, sker, kerScale, kerCenterHalf, kerSize);
+                                                     imgCenter, maskR, sker, cp, kerScale, kerCenterHalf, kerSize);
                     } else {
                         const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk,
                                            (float)volCenter, kerScale, kerCenterHalf};
                         if (inside)
-                            ref_window<TI, ONES, DENS, true, kTabRep, DW>(rw, sker, img_ptr, M, imgi, imgj, imgCenter,
-                                                                          cs, cw, img2_ptr);
+                            ref_window<TI, ONES, DENS, true, DW>(rw, sker, cp, img_ptr, M, imgi, imgj, imgCenter, cs,
+                                                                 cw, img2_ptr);
                         else
-                            ref_window<TI, ONES, DENS, false, kTabRep, DW>(rw, sker, img_ptr, M, imgi, imgj, imgCenter,
-                                                                           cs, cw, img2_ptr);
+                            ref_window<TI, ONES, DENS, false, DW>(rw, sker, cp, img_ptr, M, imgi, imgj, imgCenter, cs,
+                                                                  cw, img2_ptr);
                     }
                     // cumSumAllAxes += cumSum (gpuBackProject.cu:106), in direction order
                     wacc[l] = __fadd_rn(wacc[l], cs);
@@ -972,16 +1050,19 @@ static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *k
     constexpr int kCBZ = BpShape<ADJ, DW, DEEP>::BZ;
     const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
     const long long nb = (long long)bx * by * bz;
-    const int pad = bp_table_pad(g.ker_size, ADJ);
-    const size_t dyn = (size_t)(g.ker_size + 2 * pad) * kTabRep * sizeof(float);
+    using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
+    const BpTable tb = bp_table(g.ker_size, sizeof(Mem));
+    if (tb.copies == 0) return cudaErrorInvalidValue; // a KB table too long for shared memory
+    const size_t dyn = (size_t)tb.entries * tb.copies * sizeof(float) + kBpGroups * sizeof(Mem);
     auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
     // quad loads of image rows: 4 | M and the stacks aligned to 4 elements
     const size_t qa = 4 * sizeof(TI);
     const int vec = (g.M % 4 == 0) && ((size_t)img % qa == 0) && (!img2 || (size_t)img2 % 16 == 0) ? 1 : 0;
-    kern<<<(unsigned)nb, kCThreads, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
-                                              g.ker_hw, bx, by, pad, zero_edges ? 1 : 0, scale, img2, vec);
+    const unsigned grid = (unsigned)((nb + kBpGroups - 1) / kBpGroups);
+    kern<<<grid, kCThreads * kBpGroups, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
+                                                  g.ker_hw, bx, by, (int)nb, tb, zero_edges ? 1 : 0, scale, img2, vec);
     count_launches(1);
     return cudaGetLastError();
 }
