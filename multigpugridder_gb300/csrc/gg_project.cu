@@ -719,6 +719,39 @@ struct BpGroupMem {
     unsigned char svox[NW * WV];
 };
 
+// Bricks of x-width kCBX in row (y brick j, z brick k) that meet the sphere of
+// radius reach about the volume centre c (within the +1 margin of the test
+// d^2 <= reach^2 + 1, d the distance from the centre to the brick's box):
+// x bricks lo .. lo + n - 1.  In doubled coordinates the box's distance per
+// axis is max(|2 B i + B - 1 - 2c| - (B - 1), 0) for bricks of size B, all
+// integers, so the test is exact; along x the bricks that pass form the
+// interval |2 B i + B - 1 - 2c| <= B - 1 + t, t = isqrt(rem).
+__device__ __forceinline__ int box_dist2(int i, int B, int c)
+{
+    return max(abs(2 * B * i + B - 1 - 2 * c) - (B - 1), 0);
+}
+
+__device__ __forceinline__ int floor_div(int a, int b) { return a >= 0 ? a / b : -((-a + b - 1) / b); }
+
+__device__ void brick_row(int j, int k, int bricksX, int c, int BZ, int reach, int &lo, int &n)
+{
+    const long long dy = box_dist2(j, kCBY, c), dz = box_dist2(k, BZ, c);
+    const long long rem = 4 * ((long long)reach * reach + 1) - dy * dy - dz * dz;
+    lo = 0;
+    n = 0;
+    if (rem < 0) return;
+    long long t = (long long)sqrt((double)rem);
+    while (t * t > rem) t--;
+    while ((t + 1) * (t + 1) <= rem) t++;
+    const int B = kCBX;
+    const int ilo = max(-floor_div(-(2 * c - 2 * (B - 1) - (int)t), 2 * B), 0); // ceil
+    const int ihi = min(floor_div(2 * c + (int)t, 2 * B), bricksX - 1);
+    if (ihi >= ilo) {
+        lo = ilo;
+        n = ihi - ilo + 1;
+    }
+}
+
 __device__ __forceinline__ void group_sync(int id)
 {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(kCThreads) : "memory");
@@ -728,7 +761,7 @@ template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false, bool DEE
 __global__ void __launch_bounds__(kCThreads *kBpGroups, 1)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
-                      float kerHW, int bricksX, int bricksY, int nBricks, BpTable tb, int zeroEdges,
+                      float kerHW, int bricksX, int bricksY, BpTable tb, int zeroEdges,
                       const float *__restrict__ d_scale, const float *__restrict__ img2, int vecImg)
 {
     static_assert(!DW || (!ONES && !DENS && !ADJ), "the second image stack is a reference-rule option");
@@ -737,33 +770,56 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     constexpr int BD = Shape::BD, kWarpVox = Shape::WV, kCBZ = Shape::BZ;
     constexpr int FW = Shape::FW, FH = FW, FS = FW + 1;
     using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
-    // [table: tb.entries x tb.copies][kBpGroups x Mem]
+    // [table: tb.entries x tb.copies][kBpGroups x Mem][row starts][row prefix]
     extern __shared__ __align__(16) float bp_smem[];
     const int cp = tb.copies, tabWords = tb.entries * cp;
-    for (int t = threadIdx.x; t < tabWords; t += blockDim.x) bp_smem[t] = __ldg(ker + min(t / cp, kerSize - 1));
-    __syncthreads();
-
-    const int grp = threadIdx.x / kCThreads, brick = blockIdx.x * kBpGroups + grp;
-    if (brick >= nBricks) return;
-    Mem &sm = reinterpret_cast<Mem *>(bp_smem + tabWords)[grp];
-    float *sax = sm.sax;
-    int *slist = sm.slist, *swarp = sm.swarp;
-    const int tid = threadIdx.x - grp * kCThreads, warp = tid >> 5, lane = tid & 31;
-    const int x0 = (brick % bricksX) * kCBX;
-    const int y0 = ((brick / bricksX) % bricksY) * kCBY;
-    const int z0 = (brick / (bricksX * bricksY)) * kCBZ;
-    const int bx = x0 + (warp & 1) * 8, by = y0 + ((warp >> 1) & 1) * 4, bz = z0 + (warp >> 2) * BD;
+    Mem *gmem = reinterpret_cast<Mem *>(bp_smem + tabWords);
+    int *slo = reinterpret_cast<int *>(gmem + kBpGroups), *spre = slo + bricksY;
     const int volCenter = (int)((float)V) / 2;
     const int imgCenter = (int)((float)M) / 2;
 
-    {   // skip bricks entirely outside the mask sphere
-        const float cx = fmaxf(fabsf(x0 + 0.5f * (kCBX - 1) - volCenter) - 0.5f * (kCBX - 1), 0.f);
-        const float cy = fmaxf(fabsf(y0 + 0.5f * (kCBY - 1) - volCenter) - 0.5f * (kCBY - 1), 0.f);
-        const float cz = fmaxf(fabsf(z0 + 0.5f * (kCBZ - 1) - volCenter) - 0.5f * (kCBZ - 1), 0.f);
-        // the adjoint also reaches voxels up to 2*sqrt(3) beyond the mask sphere
-        const float reach = ADJ ? (float)maskR + 4.0f : (float)maskR;
-        if (cx * cx + cy * cy + cz * cz > reach * reach + 1.0f) return;
+    // The CTA's bricks: those of z-layer blockIdx.y that meet the sphere of
+    // radius `reach` (the adjoint reaches voxels up to 2*sqrt(3) beyond the
+    // mask), numbered row by row; the CTA takes numbers kBpGroups * blockIdx.x
+    // onward, one per group.  Row (y, z) holds the x interval [slo, slo + n).
+    const int reach = ADJ ? maskR + 4 : maskR;
+    const int kz = blockIdx.y;
+    for (int j = threadIdx.x; j < bricksY; j += blockDim.x) {
+        int lo, n;
+        brick_row(j, kz, bricksX, volCenter, kCBZ, reach, lo, n);
+        slo[j] = lo;
+        spre[j] = n;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int j = 0; j < bricksY; j++) {
+            const int c = spre[j];
+            spre[j] = acc;
+            acc += c;
+        }
+        spre[bricksY] = acc;
+    }
+    __syncthreads();
+    const int total = spre[bricksY];
+    if (kBpGroups * (int)blockIdx.x >= total) return; // the whole CTA
+    for (int t = threadIdx.x; t < tabWords; t += blockDim.x) bp_smem[t] = __ldg(ker + min(t / cp, kerSize - 1));
+    __syncthreads();
+
+    const int grp = threadIdx.x / kCThreads, a = kBpGroups * blockIdx.x + grp;
+    if (a >= total) return;
+    int row = 0; // the last row whose prefix is <= a (it holds brick a)
+    for (int hi = bricksY - 1; row < hi;) {
+        const int mid = (row + hi + 1) >> 1;
+        if (spre[mid] <= a) row = mid;
+        else hi = mid - 1;
+    }
+    Mem &sm = gmem[grp];
+    float *sax = sm.sax;
+    int *slist = sm.slist, *swarp = sm.swarp;
+    const int tid = threadIdx.x - grp * kCThreads, warp = tid >> 5, lane = tid & 31;
+    const int x0 = (slo[row] + a - spre[row]) * kCBX, y0 = row * kCBY, z0 = kz * kCBZ;
+    const int bx = x0 + (warp & 1) * 8, by = y0 + ((warp >> 1) & 1) * 4, bz = z0 + (warp >> 2) * BD;
     const float *sker = bp_smem + lane % cp; // entry k at sker[k * cp]
     const unsigned stride = 4u * (unsigned)cp;
     const unsigned tab = (unsigned)__cvta_generic_to_shared(bp_smem) + 4u * (unsigned)(lane % cp) - tb.magic_bits * stride;
@@ -1049,20 +1105,21 @@ static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *k
     if (n <= 0) return cudaSuccess;
     constexpr int kCBZ = BpShape<ADJ, DW, DEEP>::BZ;
     const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
-    const long long nb = (long long)bx * by * bz;
     using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
     const BpTable tb = bp_table(g.ker_size, sizeof(Mem));
     if (tb.copies == 0) return cudaErrorInvalidValue; // a KB table too long for shared memory
-    const size_t dyn = (size_t)tb.entries * tb.copies * sizeof(float) + kBpGroups * sizeof(Mem);
+    const size_t dyn =
+        (size_t)tb.entries * tb.copies * sizeof(float) + kBpGroups * sizeof(Mem) + (2 * (size_t)by + 1) * sizeof(int);
     auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
     // quad loads of image rows: 4 | M and the stacks aligned to 4 elements
     const size_t qa = 4 * sizeof(TI);
     const int vec = (g.M % 4 == 0) && ((size_t)img % qa == 0) && (!img2 || (size_t)img2 % 16 == 0) ? 1 : 0;
-    const unsigned grid = (unsigned)((nb + kBpGroups - 1) / kBpGroups);
+    // CTA (x, z): bricks kBpGroups x .. of z-layer z that meet the sphere
+    const dim3 grid((unsigned)((bx * by + kBpGroups - 1) / kBpGroups), (unsigned)bz);
     kern<<<grid, kCThreads * kBpGroups, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
-                                                  g.ker_hw, bx, by, (int)nb, tb, zero_edges ? 1 : 0, scale, img2, vec);
+                                                  g.ker_hw, bx, by, tb, zero_edges ? 1 : 0, scale, img2, vec);
     count_launches(1);
     return cudaGetLastError();
 }
