@@ -635,10 +635,10 @@ static int max_dyn_smem()
     return bytes;
 }
 
-// The table layout for kerSize entries beside kBpGroups working sets of
-// group_bytes: P = 512 (kerSize <= 513) or the next power of two, and as many
-// copies, 32 down to 1, as fit.  copies = 0: not even one copy fits.
-static BpTable bp_table(int kerSize, size_t group_bytes)
+// The table layout for kerSize entries beside other_bytes of shared memory:
+// P = 512 (kerSize <= 513) or the next power of two, and as many copies, 32
+// down to 1, as fit.  copies = 0: not even one copy fits.
+static BpTable bp_table(int kerSize, size_t other_bytes)
 {
     int P = 512;
     while (P < kerSize - 1) P *= 2;
@@ -649,7 +649,8 @@ static BpTable bp_table(int kerSize, size_t group_bytes)
     std::memcpy(&t.magic_bits, &t.magic, sizeof(float));
     t.copies = 32;
     const size_t limit = (size_t)max_dyn_smem();
-    while (t.copies > 0 && (size_t)t.entries * t.copies * sizeof(float) + kBpGroups * group_bytes > limit) t.copies /= 2;
+    while (t.copies > 0 && (((size_t)t.entries * t.copies + 3) & ~(size_t)3) * sizeof(float) + other_bytes > limit)
+        t.copies /= 2;
     return t;
 }
 
@@ -701,11 +702,32 @@ __device__ float adjoint_window_slow(int vi, int vj, int vk, int volCenter, floa
 // DW (reference rule, FP32 images): pd accumulates the back projection of a
 // second image stack img2 (the same directions) in the same pass, with the
 // same weights and summation order as a separate back projection of img2.
+// What a queued voxel's window needs of its direction, copied when the
+// direction's footprint is staged.
+struct alignas(16) BpDirMeta {
+    float nx0, nx1, nx2, ny0, ny1, ny2;
+    int fi0, fj0, fh, foot, dir, pad;
+};
+
+// A warp's queue of voxel windows: entries (block voxel | footprint buffer
+// << 8) in direction order, run 32 at a time, so that rounds are full across
+// directions.  NB footprint buffers per warp: 2 where shared memory allows
+// (a direction's footprint is staged while the previous direction's last
+// voxels still wait in the queue), else 1 (the queue is run empty first).
+template <bool ADJ, bool DW, bool DEEP>
+struct BpQueue {
+    static constexpr int NB = (!ADJ && !DW && !DEEP) ? 2 : 1;
+    static constexpr int NEED = (NB - 1) * 31 + BpShape<ADJ, DW, DEEP>::WV; // most entries held at once
+    static constexpr int CAP = NEED <= 128 ? 128 : (NEED <= 256 ? 256 : 512);
+};
+
 // One group's working set in shared memory (after the table).
 template <bool DENS, bool ADJ, bool DW, bool DEEP>
 struct BpGroupMem {
     using Shape = BpShape<ADJ, DW, DEEP>;
+    using Q = BpQueue<ADJ, DW, DEEP>;
     static constexpr int NW = kCThreads / 32, WV = Shape::WV, FP = Shape::FW * (Shape::FW + 1);
+    BpDirMeta smeta[NW * Q::NB];
     float sax[kBpChunk * 9];
     int slist[kBpChunk];
     int swarp[kBpChunk / 32]; // kept directions per (pass, warp)
@@ -714,9 +736,9 @@ struct BpGroupMem {
     // lane per direction, directions in order, so no atomics are needed
     float sacc[NW * WV];
     float saccw[DENS || DW ? NW * WV : 1];
-    float sfoot[NW * FP];
-    float sfoot2[DW ? NW * FP : 1];
-    unsigned char svox[NW * WV];
+    float sfoot[NW * Q::NB * FP];
+    float sfoot2[DW ? NW * Q::NB * FP : 1];
+    unsigned short squeue[NW * Q::CAP];
 };
 
 // Bricks of x-width kCBX in row (y brick j, z brick k) that meet the sphere of
@@ -773,7 +795,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     // [table: tb.entries x tb.copies][kBpGroups x Mem][row starts][row prefix]
     extern __shared__ __align__(16) float bp_smem[];
     const int cp = tb.copies, tabWords = tb.entries * cp;
-    Mem *gmem = reinterpret_cast<Mem *>(bp_smem + tabWords);
+    Mem *gmem = reinterpret_cast<Mem *>(bp_smem + ((tabWords + 3) & ~3)); // 16-byte aligned
     int *slo = reinterpret_cast<int *>(gmem + kBpGroups), *spre = slo + bricksY;
     const int volCenter = (int)((float)V) / 2;
     const int imgCenter = (int)((float)M) / 2;
@@ -823,13 +845,13 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     const float *sker = bp_smem + lane % cp; // entry k at sker[k * cp]
     const unsigned stride = 4u * (unsigned)cp;
     const unsigned tab = (unsigned)__cvta_generic_to_shared(bp_smem) + 4u * (unsigned)(lane % cp) - tb.magic_bits * stride;
-    float *sfoot = sm.sfoot, *sfoot2 = sm.sfoot2, *sacc = sm.sacc, *saccw = sm.saccw;
-    unsigned char *svox = sm.svox;
-    float *wfoot = sfoot + warp * (FH * FS);
-    float *wfoot2 = sfoot2 + (DW ? warp * (FH * FS) : 0);
-    unsigned char *wvox = svox + warp * kWarpVox;
-    float *wacc = sacc + warp * kWarpVox;
-    float *waccw = saccw + (DENS || DW ? warp * kWarpVox : 0);
+    constexpr int NB = BpQueue<ADJ, DW, DEEP>::NB, QM = BpQueue<ADJ, DW, DEEP>::CAP - 1;
+    float *const wfoot0 = sm.sfoot + warp * (NB * FH * FS);
+    float *const wfoot20 = sm.sfoot2 + (DW ? warp * (NB * FH * FS) : 0);
+    BpDirMeta *const wmeta = sm.smeta + warp * NB;
+    unsigned short *const wq = sm.squeue + warp * (QM + 1);
+    float *const wacc = sm.sacc + warp * kWarpVox;
+    float *const waccw = sm.saccw + (DENS || DW ? warp * kWarpVox : 0);
 
     // this lane's voxels: x = lx, y = ly, z = bz + s
     const int lx = bx + (lane & 7), ly = by + (lane >> 3);
@@ -859,6 +881,82 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     const float bcx = x0 + 0.5f * (kCBX - 1) - volCenter, bcy = y0 + 0.5f * (kCBY - 1) - volCenter,
                 bcz = z0 + 0.5f * (kCBZ - 1) - volCenter;
     const unsigned lt_mask = (1u << lane) - 1u;
+    int qhead = 0, qsize = 0, nbuf = 0; // the warp's queue (uniform)
+
+    // One voxel's window sum for one direction: the fast window from the
+    // footprint, or the reference's (or the adjoint's) window from the image.
+    auto voxel_window = [&](const int l, const float nx0, const float nx1, const float nx2, const float ny0,
+                            const float ny1, const float ny2, const int fi0, const int fj0, const int fh,
+                            const bool foot, const TI *img_ptr, const float *img2_ptr, const float *wfoot,
+                            const float *wfoot2, float &cs, float &cw) {
+        const int vi = bx + (l & 7), vj = by + ((l >> 3) & 3), vk = bz + (l >> 5);
+        const float a0 = (float)vi - volCenter, a1 = (float)vj - volCenter, a2 = (float)vk - volCenter;
+        const float f_imgi = __fadd_rn(voxel_proj(a0, a1, a2, nx0, nx1, nx2), (float)imgCenter);
+        const float f_imgj = __fadd_rn(voxel_proj(a0, a1, a2, ny0, ny1, ny2), (float)imgCenter);
+        const int imgi = (int)roundf(f_imgi);
+        const int imgj = (int)roundf(f_imgj);
+        const bool inside = imgi >= 2 && imgj >= 2 && imgi + 2 < M && imgj + 2 < M;
+        const int ri = imgi - HALF - fi0, rj = imgj - HALF - fj0;
+        if (foot && (unsigned)ri <= (unsigned)(FW - W) && (unsigned)rj <= (unsigned)(fh - W) && vi >= 4 &&
+            vj >= 4 && vk >= 4 && (ADJ || inside || !DENS)) {
+            // reference rule: index of r = Q - v; adjoint: of r = v - Q
+            const float sg = ADJ ? -kerScale : kerScale;
+            // scaled by 1/P (exact): the saturating index form
+            const FootWin fwin{nx0, nx1, nx2, ny0, ny1, ny2, (float)volCenter, sg * tb.scale,
+                               (kerCenterHalf - (float)vi * sg) * tb.scale,
+                               (kerCenterHalf - (float)vj * sg) * tb.scale,
+                               (kerCenterHalf - (float)vk * sg) * tb.scale, tb.magic, stride};
+            const float *fb = wfoot + rj * FS + ri;
+            const float pi0 = (float)(imgi - HALF - imgCenter), pj0 = (float)(imgj - HALF - imgCenter);
+            foot_window_x2<DENS, W, W, FS, DW>(fwin, fb, tab, pi0, pj0, cs, cw,
+                                            DW ? wfoot2 + rj * FS + ri : nullptr);
+        } else if (ADJ) {
+            cs = adjoint_window_slow<TI>(vi, vj, vk, volCenter, nx0, nx1, nx2, ny0, ny1, ny2, img_ptr, M,
+                                         imgCenter, maskR, sker, cp, kerScale, kerCenterHalf, kerSize);
+        } else {
+            const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk,
+                               (float)volCenter, kerScale, kerCenterHalf};
+            if (inside)
+                ref_window<TI, ONES, DENS, true, DW>(rw, sker, cp, img_ptr, M, imgi, imgj, imgCenter, cs, cw,
+                                                     img2_ptr);
+            else
+                ref_window<TI, ONES, DENS, false, DW>(rw, sker, cp, img_ptr, M, imgi, imgj, imgCenter, cs, cw,
+                                                      img2_ptr);
+        }
+    };
+
+    // One round of the queue (NB = 2): its first cnt (<= 32) voxels, one per
+    // lane.  Each voxel's window sum is added to its total in direction
+    // order: the round holds at most one direction per buffer, the older
+    // one's first.
+    auto run_round = [&](const int cnt) {
+        float cs = 0.0f, cw = 0.0f;
+        int l = 0, b = 0;
+        if (lane < cnt) {
+            const unsigned ent = wq[(qhead + lane) & QM];
+            l = ent & 0xff;
+            b = ent >> 8;
+            const BpDirMeta m = wmeta[b];
+            voxel_window(l, m.nx0, m.nx1, m.nx2, m.ny0, m.ny1, m.ny2, m.fi0, m.fj0, m.fh, m.foot != 0,
+                         img + (size_t)m.dir * MM, DW ? img2 + (size_t)m.dir * MM : nullptr, wfoot0 + b * (FH * FS),
+                         wfoot20 + (DW ? b * (FH * FS) : 0), cs, cw);
+        }
+        // cumSumAllAxes += cumSum (gpuBackProject.cu:106), in direction order
+        const int bf = wq[qhead & QM] >> 8;
+        if (lane < cnt && b == bf) {
+            wacc[l] = __fadd_rn(wacc[l], cs);
+            if (DENS || DW) waccw[l] = __fadd_rn(waccw[l], cw);
+        }
+        __syncwarp();
+        if (lane < cnt && b != bf) {
+            wacc[l] = __fadd_rn(wacc[l], cs);
+            if (DENS || DW) waccw[l] = __fadd_rn(waccw[l], cw);
+        }
+        __syncwarp(); // the entries, buffers and sums are free again
+        qhead = (qhead + cnt) & QM;
+        qsize -= cnt;
+    };
+
     for (int c0 = 0; c0 < n; c0 += kBpChunk) {
         const int cn = min(kBpChunk, n - c0);
         group_sync(grp + 1);
@@ -930,24 +1028,31 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 if (fabsf(d) > slab + ext) continue;
             }
             // the reference's per-voxel slab test (gpuBackProject.cu:64-66), or
-            // the adjoint's reach; the active voxels are listed slot by slot,
-            // in lane order
+            // the adjoint's reach
+            unsigned actm = 0;
             int total = 0;
 #pragma unroll
             for (int s = 0; s < BD; s++) {
                 const float az = (float)(bz + s) - volCenter;
                 const float fk = voxel_proj(ax0, ay0, az, nz0, nz1, nz2);
                 const bool act = ((inmask >> s) & 1u) && (ADJ ? fabsf(fk) < slabD : fabsf(fk) <= kerHW);
-                const unsigned bal = __ballot_sync(0xffffffffu, act);
-                if (act) wvox[total + __popc(bal & lt_mask)] = (unsigned char)(lane + 32 * s);
-                total += __popc(bal);
+                actm |= (act ? 1u : 0u) << s;
+                total += __popc(__ballot_sync(0xffffffffu, act));
             }
             if (total == 0) continue;
+            int b = 0;
+            if (NB > 1) {
+                b = nbuf;
+                nbuf ^= 1;
+                // buffer b's earlier voxels (all at the front of the queue) run first
+                while (qsize > 0 && (wq[qhead & QM] >> 8) == b) run_round(min(qsize, 32));
+            }
+            float *const wfoot = wfoot0 + b * (FH * FS);
+            float *const wfoot2 = wfoot20 + (DW ? b * (FH * FS) : 0);
             const float nx0 = ax[0], nx1 = ax[1], nx2 = ax[2];
             const float ny0 = ax[3], ny1 = ax[4], ny2 = ax[5];
             const TI *img_ptr = img + (size_t)(c0 + al) * MM;
             const float *img2_ptr = DW ? img2 + (size_t)(c0 + al) * MM : nullptr;
-
             // this warp's footprint (uniform across the warp)
             int fi0 = 0, fj0 = 0, fh = 0;
             bool foot = false;
@@ -1037,55 +1142,50 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                     }
                 }
             }
-            __syncwarp();  // the voxel list and the footprint are complete
-
-            for (int base = 0; base < total; base += 32) {
-                const int t = base + lane;
-                if (t < total) {
-                    float cs = 0.0f, cw = 0.0f;
-                    const int l = wvox[t];
-                    const int vi = bx + (l & 7), vj = by + ((l >> 3) & 3), vk = bz + (l >> 5);
-                    const float a0 = (float)vi - volCenter, a1 = (float)vj - volCenter, a2 = (float)vk - volCenter;
-                    const float f_imgi = __fadd_rn(voxel_proj(a0, a1, a2, nx0, nx1, nx2), (float)imgCenter);
-                    const float f_imgj = __fadd_rn(voxel_proj(a0, a1, a2, ny0, ny1, ny2), (float)imgCenter);
-                    const int imgi = (int)roundf(f_imgi);
-                    const int imgj = (int)roundf(f_imgj);
-                    const bool inside = imgi >= 2 && imgj >= 2 && imgi + 2 < M && imgj + 2 < M;
-                    const int ri = imgi - HALF - fi0, rj = imgj - HALF - fj0;
-                    if (foot && (unsigned)ri <= (unsigned)(FW - W) && (unsigned)rj <= (unsigned)(fh - W) &&
-                        vi >= 4 && vj >= 4 && vk >= 4 && (ADJ || inside || !DENS)) {
-                        // reference rule: index of r = Q - v; adjoint: of r = v - Q
-                        const float sg = ADJ ? -kerScale : kerScale;
-                        // scaled by 1/P (exact): the saturating index form
-                        const FootWin fwin{nx0, nx1, nx2, ny0, ny1, ny2, (float)volCenter, sg * tb.scale,
-                                           (kerCenterHalf - (float)vi * sg) * tb.scale,
-                                           (kerCenterHalf - (float)vj * sg) * tb.scale,
-                                           (kerCenterHalf - (float)vk * sg) * tb.scale, tb.magic, stride};
-                        const float *fb = wfoot + rj * FS + ri;
-                        const float pi0 = (float)(imgi - HALF - imgCenter), pj0 = (float)(imgj - HALF - imgCenter);
-                        foot_window_x2<DENS, W, W, FS, DW>(fwin, fb, tab, pi0, pj0, cs, cw,
-                                                        DW ? wfoot2 + rj * FS + ri : nullptr);
-                    } else if (ADJ) {
-                        cs = adjoint_window_slow<TI>(vi, vj, vk, volCenter, nx0, nx1, nx2, ny0, ny1, ny2, img_ptr, M,
-                                                     imgCenter, maskR, sker, cp, kerScale, kerCenterHalf, kerSize);
-                    } else {
-                        const RefWindow rw{nx0, nx1, nx2, ny0, ny1, ny2, (float)vi, (float)vj, (float)vk,
-                                           (float)volCenter, kerScale, kerCenterHalf};
-                        if (inside)
-                            ref_window<TI, ONES, DENS, true, DW>(rw, sker, cp, img_ptr, M, imgi, imgj, imgCenter, cs,
-                                                                 cw, img2_ptr);
-                        else
-                            ref_window<TI, ONES, DENS, false, DW>(rw, sker, cp, img_ptr, M, imgi, imgj, imgCenter, cs,
-                                                                  cw, img2_ptr);
-                    }
-                    // cumSumAllAxes += cumSum (gpuBackProject.cu:106), in direction order
-                    wacc[l] = __fadd_rn(wacc[l], cs);
-                    if (DENS || DW) waccw[l] = __fadd_rn(waccw[l], cw);
+            if (NB > 1) {
+                if (lane == 0)
+                    wmeta[b] = BpDirMeta{nx0, nx1, nx2, ny0, ny1, ny2, fi0, fj0, fh, foot ? 1 : 0, c0 + al, 0};
+                // the active voxels join the queue slot by slot, in lane order
+                int pos = qhead + qsize;
+#pragma unroll
+                for (int s = 0; s < BD; s++) {
+                    const bool act = (actm >> s) & 1u;
+                    const unsigned bal = __ballot_sync(0xffffffffu, act);
+                    if (act) wq[(pos + __popc(bal & lt_mask)) & QM] = (unsigned short)((lane + 32 * s) | (b << 8));
+                    pos += __popc(bal);
                 }
+                qsize += total;
+                __syncwarp(); // the queue entries, the footprint and its record are complete
+                while (qsize >= 32) run_round(32);
+            } else {
+                // the active voxels, slot by slot in lane order, run at once
+                int pos = 0;
+#pragma unroll
+                for (int s = 0; s < BD; s++) {
+                    const bool act = (actm >> s) & 1u;
+                    const unsigned bal = __ballot_sync(0xffffffffu, act);
+                    if (act) wq[pos + __popc(bal & lt_mask)] = (unsigned short)(lane + 32 * s);
+                    pos += __popc(bal);
+                }
+                __syncwarp(); // the voxel list and the footprint are complete
+                for (int base = 0; base < total; base += 32) {
+                    const int t = base + lane;
+                    if (t < total) {
+                        float cs = 0.0f, cw = 0.0f;
+                        const int l = wq[t];
+                        voxel_window(l, nx0, nx1, nx2, ny0, ny1, ny2, fi0, fj0, fh, foot, img_ptr, img2_ptr, wfoot,
+                                     wfoot2, cs, cw);
+                        // cumSumAllAxes += cumSum (gpuBackProject.cu:106), in direction order
+                        wacc[l] = __fadd_rn(wacc[l], cs);
+                        if (DENS || DW) waccw[l] = __fadd_rn(waccw[l], cw);
+                    }
+                }
+                __syncwarp(); // the next direction rewrites the list, the footprint and these sums
             }
-            __syncwarp();  // the next direction rewrites the list, the footprint and these sums
         }
     }
+    if (NB > 1)
+        while (qsize > 0) run_round(min(qsize, 32));
     __syncwarp();
     const float sc = d_scale ? *d_scale : 1.0f;
 #pragma unroll
@@ -1106,10 +1206,10 @@ static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *k
     constexpr int kCBZ = BpShape<ADJ, DW, DEEP>::BZ;
     const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
     using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
-    const BpTable tb = bp_table(g.ker_size, sizeof(Mem));
+    const size_t other = kBpGroups * sizeof(Mem) + (2 * (size_t)by + 1) * sizeof(int);
+    const BpTable tb = bp_table(g.ker_size, other);
     if (tb.copies == 0) return cudaErrorInvalidValue; // a KB table too long for shared memory
-    const size_t dyn =
-        (size_t)tb.entries * tb.copies * sizeof(float) + kBpGroups * sizeof(Mem) + (2 * (size_t)by + 1) * sizeof(int);
+    const size_t dyn = (((size_t)tb.entries * tb.copies + 3) & ~(size_t)3) * sizeof(float) + other;
     auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
