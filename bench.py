@@ -283,7 +283,7 @@ def run_gb300(args):
     # capture of this workload at full size; null for other shapes
     traffic = None
     if dom == "back" and fused and N == 128 and args.batch == 2000 and args.precision == "f32" and n == 10000:
-        traffic = 2.07e9
+        traffic = 1.74e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": "measured" if peaks.get("hbm_gbs") else "fallback",
                 "traffic": traffic, "bytes_per_unit": bpu[dom], "units_per_launch": units_per_launch,
