@@ -56,10 +56,12 @@ cudaError_t launch_pitch_volume(const float *d_cas, int V, int P, void *d_out, i
 // FP32 CAS volume.  d_img holds n*M*M CAS images in storage `iprec`; when
 // `ones` is set the images are taken to be all ones (plane density) and
 // d_img is not read.
-// *d_scale multiplies each voxel's sum before it is added.
+// *d_scale multiplies each voxel's sum before it is added.  shared: the GPU
+// runs other launches concurrently (smaller CTAs that share an SM; FP32
+// images, the same sums bit for bit).
 cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, bool ones,
                                     const float *d_ker, const float *d_axes, int n, const Geom &g,
-                                    const float *d_scale, cudaStream_t s);
+                                    const float *d_scale, cudaStream_t s, bool shared = false);
 
 // Reference-rule back projection of d_img into d_vol and, in the same pass,
 // of all-ones images (the plane density) into d_pd; both accumulated.

@@ -9,7 +9,9 @@
 // centre M/2, nearest-index lookup into the KB table, int mask radius.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "gg_common.cuh"
 #include "gg_internal.h"
@@ -638,7 +640,7 @@ static int max_dyn_smem()
 // The table layout for kerSize entries beside other_bytes of shared memory:
 // P = 512 (kerSize <= 513) or the next power of two, and as many copies, 32
 // down to 1, as fit.  copies = 0: not even one copy fits.
-static BpTable bp_table(int kerSize, size_t other_bytes)
+static BpTable bp_table(int kerSize, size_t other_bytes, int max_copies = 32, size_t limit_bytes = 0)
 {
     int P = 512;
     while (P < kerSize - 1) P *= 2;
@@ -647,8 +649,8 @@ static BpTable bp_table(int kerSize, size_t other_bytes)
     t.scale = 1.0f / (float)P;
     t.magic = 12582912.0f / (float)P;
     std::memcpy(&t.magic_bits, &t.magic, sizeof(float));
-    t.copies = 32;
-    const size_t limit = (size_t)max_dyn_smem();
+    t.copies = max_copies;
+    const size_t limit = limit_bytes ? limit_bytes : (size_t)max_dyn_smem();
     while (t.copies > 0 && (((size_t)t.entries * t.copies + 3) & ~(size_t)3) * sizeof(float) + other_bytes > limit)
         t.copies /= 2;
     return t;
@@ -779,8 +781,8 @@ __device__ __forceinline__ void group_sync(int id)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(kCThreads) : "memory");
 }
 
-template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false, bool DEEP = false>
-__global__ void __launch_bounds__(kCThreads *kBpGroups, 1)
+template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false, bool DEEP = false, int G = kBpGroups>
+__global__ void __launch_bounds__(kCThreads *G, G == 1 ? 3 : 1)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
                       float kerHW, int bricksX, int bricksY, BpTable tb, int zeroEdges,
@@ -792,17 +794,17 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     constexpr int BD = Shape::BD, kWarpVox = Shape::WV, kCBZ = Shape::BZ;
     constexpr int FW = Shape::FW, FH = FW, FS = FW + 1;
     using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
-    // [table: tb.entries x tb.copies][kBpGroups x Mem][row starts][row prefix]
+    // [table: tb.entries x tb.copies][G x Mem][row starts][row prefix]
     extern __shared__ __align__(16) float bp_smem[];
     const int cp = tb.copies, tabWords = tb.entries * cp;
     Mem *gmem = reinterpret_cast<Mem *>(bp_smem + ((tabWords + 3) & ~3)); // 16-byte aligned
-    int *slo = reinterpret_cast<int *>(gmem + kBpGroups), *spre = slo + bricksY;
+    int *slo = reinterpret_cast<int *>(gmem + G), *spre = slo + bricksY;
     const int volCenter = (int)((float)V) / 2;
     const int imgCenter = (int)((float)M) / 2;
 
     // The CTA's bricks: those of z-layer blockIdx.y that meet the sphere of
     // radius `reach` (the adjoint reaches voxels up to 2*sqrt(3) beyond the
-    // mask), numbered row by row; the CTA takes numbers kBpGroups * blockIdx.x
+    // mask), numbered row by row; the CTA takes numbers G * blockIdx.x
     // onward, one per group.  Row (y, z) holds the x interval [slo, slo + n).
     const int reach = ADJ ? maskR + 4 : maskR;
     const int kz = blockIdx.y;
@@ -824,20 +826,20 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     }
     __syncthreads();
     const int total = spre[bricksY];
-    if ((DEEP ? 2 : 1) * kBpGroups * (int)blockIdx.x >= total) return; // the whole CTA
+    if (((DEEP && G > 1) ? 2 : 1) * G * (int)blockIdx.x >= total) return; // the whole CTA
     for (int t = threadIdx.x; t < tabWords; t += blockDim.x) bp_smem[t] = __ldg(ker + min(t / cp, kerSize - 1));
     __syncthreads();
 
-    // Group g runs brick g of the CTA's run of RUN * kBpGroups bricks, and
-    // with 8-deep blocks (RUN = 2) then brick 2 kBpGroups - 1 - g: along a run
+    // Group g runs brick g of the CTA's run of RUN * G bricks, and
+    // with 8-deep blocks (RUN = 2) then brick 2 G - 1 - g: along a run
     // the work drifts (about 2/r of the directions reach a voxel at radius r),
     // and the mirrored pairs even it out.  On 512^2 images that measured 2-3%
     // faster; on 256^2 images 8% slower, as the groups drift apart in time and
     // lose the L1 reuse of the neighbouring bricks' footprints.
-    constexpr int RUN = DEEP ? 2 : 1;
+    constexpr int RUN = (DEEP && G > 1) ? 2 : 1;
     const int grp = threadIdx.x / kCThreads;
     for (int pass = 0; pass < RUN; pass++) {
-        const int a = RUN * kBpGroups * blockIdx.x + (pass == 0 ? grp : RUN * kBpGroups - 1 - grp);
+        const int a = RUN * G * blockIdx.x + (pass == 0 ? grp : RUN * G - 1 - grp);
         if (a >= total) break;
         int row = 0; // the last row whose prefix is <= a (it holds brick a)
         for (int hi = bricksY - 1; row < hi;) {
@@ -1207,50 +1209,75 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     }
 }
 
-template <typename TI, bool ONES, bool DENS = false, bool ADJ = false, bool DW = false, bool DEEP = false>
-static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
-                                       const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr,
-                                       bool zero_edges = true, const float *img2 = nullptr)
+template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW, bool DEEP, int G>
+static cudaError_t launch_bp_compact_g(float *vol, const TI *img, const float *ker, const float *axes, int n,
+                                       const Geom &g, const float *scale, cudaStream_t s, float *pd, bool zero_edges,
+                                       const float *img2, int max_copies)
 {
-    if (n <= 0) return cudaSuccess;
     constexpr int kCBZ = BpShape<ADJ, DW, DEEP>::BZ;
     const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
     using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
-    const size_t other = kBpGroups * sizeof(Mem) + (2 * (size_t)by + 1) * sizeof(int);
-    const BpTable tb = bp_table(g.ker_size, other);
+    const size_t other = G * sizeof(Mem) + (2 * (size_t)by + 1) * sizeof(int);
+    // one group per CTA: three CTAs an SM (228 KB, 1 KB reserved per CTA)
+    const size_t limit = G == 1 ? (size_t)(228 * 1024 / 3 - 1024) : 0;
+    const BpTable tb = bp_table(g.ker_size, other, max_copies, limit);
     if (tb.copies == 0) return cudaErrorInvalidValue; // a KB table too long for shared memory
     const size_t dyn = (((size_t)tb.entries * tb.copies + 3) & ~(size_t)3) * sizeof(float) + other;
-    auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP>;
+    auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return e;
     // quad loads of image rows: 4 | M and the stacks aligned to 4 elements
     const size_t qa = 4 * sizeof(TI);
     const int vec = (g.M % 4 == 0) && ((size_t)img % qa == 0) && (!img2 || (size_t)img2 % 16 == 0) ? 1 : 0;
     // CTA (x, z): bricks run x .. of z-layer z that meet the sphere
-    const int run = (DEEP ? 2 : 1) * kBpGroups;
+    const int run = ((DEEP && G > 1) ? 2 : 1) * G;
     const dim3 grid((unsigned)((bx * by + run - 1) / run), (unsigned)bz);
-    kern<<<grid, kCThreads * kBpGroups, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
-                                                  g.ker_hw, bx, by, tb, zero_edges ? 1 : 0, scale, img2, vec);
+    kern<<<grid, kCThreads * G, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size, g.ker_hw,
+                                          bx, by, tb, zero_edges ? 1 : 0, scale, img2, vec);
     count_launches(1);
     return cudaGetLastError();
+}
+
+template <typename TI, bool ONES, bool DENS = false, bool ADJ = false, bool DW = false, bool DEEP = false>
+static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *ker, const float *axes, int n,
+                                       const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr,
+                                       bool zero_edges = true, const float *img2 = nullptr, bool shared = false)
+{
+    if (n <= 0) return cudaSuccess;
+    // A GPU shared with concurrent launches (the serving lanes): one group
+    // and one table copy per CTA, three CTAs an SM, which the launches of
+    // other lanes can fill as they free (serving capacity 172 -> 195 req/s);
+    // alone, three groups sharing 32 table copies (batched back projection
+    // 78.5 -> 71.7 ms per 10k images).
+    if constexpr (std::is_same<TI, float>::value && !ONES && !DENS && !ADJ && !DW) {
+        if (shared)
+            return launch_bp_compact_g<TI, ONES, DENS, ADJ, DW, DEEP, 1>(vol, img, ker, axes, n, g, scale, s, pd,
+                                                                         zero_edges, img2, 1);
+    }
+    return launch_bp_compact_g<TI, ONES, DENS, ADJ, DW, DEEP, kBpGroups>(vol, img, ker, axes, n, g, scale, s, pd,
+                                                                         zero_edges, img2, 32);
 }
 
 // Reference-rule launch with the block depth chosen by the image size.
 template <typename TI, bool ONES, bool DENS>
 static cudaError_t launch_bp_ref_sized(float *vol, const TI *img, const float *ker, const float *axes, int n,
-                                       const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr)
+                                       const Geom &g, const float *scale, cudaStream_t s, float *pd = nullptr,
+                                       bool shared = false)
 {
     if (g.M >= 512)
-        return launch_bp_compact_t<TI, ONES, DENS, false, false, true>(vol, img, ker, axes, n, g, scale, s, pd);
-    return launch_bp_compact_t<TI, ONES, DENS>(vol, img, ker, axes, n, g, scale, s, pd);
+        return launch_bp_compact_t<TI, ONES, DENS, false, false, true>(vol, img, ker, axes, n, g, scale, s, pd, true,
+                                                                        nullptr, shared);
+    return launch_bp_compact_t<TI, ONES, DENS>(vol, img, ker, axes, n, g, scale, s, pd, true, nullptr, shared);
 }
 
 cudaError_t launch_back_project_ref(float *d_vol, const void *d_img, int iprec, bool ones, const float *d_ker,
-                                    const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s)
+                                    const float *d_axes, int n, const Geom &g, const float *scale, cudaStream_t s,
+                                    bool shared)
 {
     if (ones) return launch_bp_ref_sized<float, true, false>(d_vol, nullptr, d_ker, d_axes, n, g, scale, s);
     if (iprec == kF32)
-        return launch_bp_ref_sized<float, false, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s);
+        return launch_bp_ref_sized<float, false, false>(d_vol, (const float *)d_img, d_ker, d_axes, n, g, scale, s,
+                                                        nullptr, shared);
     if (iprec == kF16)
         return launch_bp_ref_sized<__half, false, false>(d_vol, (const __half *)d_img, d_ker, d_axes, n, g, scale, s);
     return launch_bp_ref_sized<__nv_bfloat16, false, false>(d_vol, (const __nv_bfloat16 *)d_img, d_ker, d_axes, n, g,

@@ -271,7 +271,7 @@ void enqueue(gg_server *S, Request &r)
                 GS_CK(launch_spectrum_to_cas_images(d_spec, v.M, b, d_cas, kF32, nullptr, s));
             }
             GS_CK(launch_back_project_ref(d_acc, d_cas, kF32, false, v.ker, d_axes + (size_t)c0 * 9, b, v.g, nullptr,
-                                          s));
+                                          s, true));
         }
     }
     if (r.op == GG_OP_BACK) {

@@ -79,6 +79,39 @@ def test_back_kernel_matches_oracle(cuda, gglib, N):
     assert np.all(got[ref == 0] == 0)
 
 
+def _table(kind):
+    """KB tables of other lengths (getKernelFiltTable's size argument), and a
+    raw window whose edge entries are not zero."""
+    if kind == "raw":
+        x = np.linspace(-2.0, 2.0, 501)
+        return (O.grid_lib_kaiser(2, O.kernel_alpha(2), x) + 0.05).astype(np.float32)
+    return O.kb_table(2, int(kind)).astype(np.float32)
+
+
+@pytest.mark.parametrize("kind", ["1000", "513", "101", "raw"])
+def test_back_kernel_other_tables_bit_exact(cuda, gglib, kind):
+    """The back projection's saturating table index and its interleaved table
+    copies (P = 512 or 1024 entries, 32 or 16 copies) for tables of other
+    lengths, and the clamp to the edge entries for a table whose edges are not
+    zero: equal to the oracle's FP32 restatement bit for bit."""
+    import torch
+
+    N = 32
+    p = O.Params(N)
+    ker = _table(kind)
+    rng = np.random.default_rng(11)
+    axes = test_axes(6, seed=3)[:10]
+    img = rng.standard_normal((len(axes), p.M, p.M)).astype(np.float32)
+    ref = O.bp_ref_f32(img, axes, p.V, p.mask_radius, ker)
+    vol = torch.zeros((p.V,) * 3, device=cuda)
+    d_img, d_ker, d_axes = to_dev(img, cuda), to_dev(ker, cuda), to_dev(axes, cuda)
+    rc = gglib.gg_back_project_kernel(dptr(vol), dptr(d_img), dptr(d_ker), dptr(d_axes), 2.0, len(axes), p.V, p.M,
+                                      p.mask_radius, ker.size, 3, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(vol.cpu().numpy(), ref)
+
+
 def test_back_kernel_deep_blocks_bit_exact(cuda, gglib):
     """CAS images of 512^2 (N = 256) take the 8-voxel-deep warp blocks: the
     back projection equals the oracle's FP32 restatement bit for bit."""
