@@ -112,6 +112,27 @@ def test_back_kernel_other_tables_bit_exact(cuda, gglib, kind):
     assert np.array_equal(vol.cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("N", [21, 50, 100])
+def test_back_kernel_other_sizes_bit_exact(cuda, gglib, N):
+    """Volume edges whose CAS images are not a multiple of 4 wide (M = 42:
+    footprints staged pixel by pixel), and brick grids that do not divide the
+    CAS volume (V = 48, 106, 206): equal to the oracle bit for bit."""
+    import torch
+
+    p = O.Params(N)
+    rng = np.random.default_rng(300 + N)
+    axes = test_axes(5, seed=N)[:8]
+    img = rng.standard_normal((len(axes), p.M, p.M)).astype(np.float32)
+    ref = O.bp_ref_f32(img, axes, p.V, p.mask_radius, p.ker)
+    vol = torch.zeros((p.V,) * 3, device=cuda)
+    d_img, d_ker, d_axes = to_dev(img, cuda), to_dev(p.ker, cuda), to_dev(axes, cuda)
+    rc = gglib.gg_back_project_kernel(dptr(vol), dptr(d_img), dptr(d_ker), dptr(d_axes), 2.0, len(axes), p.V, p.M,
+                                      p.mask_radius, p.ker.size, 3, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(vol.cpu().numpy(), ref)
+
+
 def test_back_kernel_deep_blocks_bit_exact(cuda, gglib):
     """CAS images of 512^2 (N = 256) take the 8-voxel-deep warp blocks: the
     back projection equals the oracle's FP32 restatement bit for bit."""
@@ -299,10 +320,10 @@ def test_forward_project_pinned_outputs(cuda):
         assert np.array_equal(cas.numpy(), g.forwardProjectCAS(axes))
 
 
-def test_reconstruct_volume(cuda):
+@pytest.mark.parametrize("N", [32, 50])
+def test_reconstruct_volume(cuda, N):
     import multigpugridder_gb300 as gg
 
-    N = 32
     p = O.Params(N)
     vol = O.blob_volume(N, 10, seed=21)
     axes = test_axes(30, seed=22)
