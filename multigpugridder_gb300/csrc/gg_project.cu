@@ -350,8 +350,8 @@ cudaError_t launch_forward_project(const void *d_vol, int vprec, int pitch, floa
 // ---------------------------------------------------------------------------
 // Back projection: the reference window and shared constants
 // ---------------------------------------------------------------------------
-// Directions are staged through shared memory in chunks of kBpChunk, one per
-// thread of a CTA for the cull.
+// Directions are staged through shared memory in chunks of kBpChunk, two per
+// thread of a brick group for the cull.
 constexpr int kBpChunk = 512;
 
 // Conservative reach of the slab test: fp32 rounding of f_imgk is far below this.
@@ -439,7 +439,7 @@ static_assert(kBpChunk % kCThreads == 0, "the cull gives each thread kBpChunk / 
 // fits 16 pixels for any orthonormal axes (2 |(3.5, 1.5, 2.5)| + 1.2 < 11).
 // The adjoint keeps 4 (6-deep blocks fit its 24-wide footprint but measured
 // 4% slower on the gradient step), and so does the two-stack form (6-deep
-// fits its 48 KB of static shared memory but measured no faster).
+// blocks measured no faster there).
 template <bool ADJ, bool DW, bool DEEP>
 struct BpShape {
     static constexpr int BD = (ADJ || DW) ? 4 : (DEEP ? 8 : 6);
@@ -460,9 +460,11 @@ struct BpShape {
 // the same end of the table as the reference's clamp, and a table of P + 1
 // entries that repeats the last one past kerSize - 1 gives the clamped
 // entry.  floor(P y) is the low bits of y + 1.5*2^23/P added with round-down.
-// Checked on the CPU against the reference formula for every float Q within
-// 4.2 of v (v = 4..40; tables of 501 and 1000 entries) and on random samples
-// up to v = 600: identical entries.
+// The unscaled index was checked on the CPU against the reference formula for
+// every float Q within 4.2 of v (v = 4..40; tables of 501 and 1000 entries);
+// the scaled, clamped entry on 1.4e8 values of Q within 4.2 of v (v up to
+// 600), both neighbours of every index boundary among them, for tables of
+// 501, 1000, 101 and 513 entries: identical entries.
 //
 // The table is held in `copies` interleaved copies (entry k of copy c at word
 // k * copies + c) and lane l reads copy l % copies.  With 32 copies (66 KB
@@ -804,8 +806,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
 
     // The CTA's bricks: those of z-layer blockIdx.y that meet the sphere of
     // radius `reach` (the adjoint reaches voxels up to 2*sqrt(3) beyond the
-    // mask), numbered row by row; the CTA takes numbers G * blockIdx.x
-    // onward, one per group.  Row (y, z) holds the x interval [slo, slo + n).
+    // mask), numbered row by row; the CTA takes the run of RUN * G numbers
+    // from RUN * G * blockIdx.x (below).  Row (y, z) holds the x interval
+    // [slo, slo + n).
     const int reach = ADJ ? maskR + 4 : maskR;
     const int kz = blockIdx.y;
     for (int j = threadIdx.x; j < bricksY; j += blockDim.x) {
