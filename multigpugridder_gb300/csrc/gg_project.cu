@@ -426,23 +426,24 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
 // kernel's loops, bit for bit.  A CTA holds kBpGroups groups on neighbouring
 // bricks, which share one copy of the KB table (below); each group
 // synchronises on its own named barrier.
-constexpr int kCBX = 16, kCBY = 8; // brick: 2x2x2 warp blocks of 8x4xBD (BD = 8, or 4 for ADJ / DW)
+constexpr int kCBX = 16, kCBY = 8; // brick: 2x2x2 warp blocks of 8x4xBD (BD = 6, or 8 on large images)
 constexpr int kCThreads = 256;  // threads of a group
 constexpr int kBpGroups = 3;    // groups (bricks) per CTA, one CTA per SM
 static_assert(kBpChunk % kCThreads == 0, "the cull gives each thread kBpChunk / kCThreads directions");
-// Depth of a warp block for the reference rule: 6 voxels, or 8 (DEEP) on CAS
-// images of 512^2 and more.  Deeper blocks have more active voxels per
-// direction (fewer idle lanes in the last round of 32) and stage a footprint
-// for more voxels, which pays most where the images are large (each staging
-// reads from L2 or DRAM); on 256^2 images 8-deep blocks measured 20% slower
-// than 4-deep ones and 6-deep ones 0.7% faster.  With 6 the footprint still
-// fits 16 pixels for any orthonormal axes (2 |(3.5, 1.5, 2.5)| + 1.2 < 11).
-// The adjoint keeps 4 (6-deep blocks fit its 24-wide footprint but measured
-// 4% slower on the gradient step), and so does the two-stack form (6-deep
-// blocks measured no faster there).
+// Depth of a warp block: 6 voxels, or 8 (DEEP, reference rule) on CAS images
+// of 512^2 and more.  Deeper blocks have more active voxels per direction
+// (fewer idle lanes in the last round of 32) and stage a footprint for more
+// voxels, which pays most where the images are large (each staging reads from
+// L2 or DRAM); on 256^2 images 8-deep blocks measured 20% slower than 4-deep
+// ones and 6-deep ones 0.7% faster.  With 6 the footprint still fits 16
+// pixels for any orthonormal axes (2 |(3.5, 1.5, 2.5)| + 1.2 < 11), and the
+// adjoint's 7x7 windows fit 24.  The adjoint and the two-stack form had 4
+// while their 256-thread CTAs held a padded table each; with the shared table
+// copies 6-deep blocks measured faster for both (gradient step 89.6 -> 87.4
+// ms, CTF-corrected reconstructVol 88.6 -> 84.1 ms).
 template <bool ADJ, bool DW, bool DEEP>
 struct BpShape {
-    static constexpr int BD = (ADJ || DW) ? 4 : (DEEP ? 8 : 6);
+    static constexpr int BD = DEEP ? 8 : 6;
     static constexpr int WV = 32 * BD;                         // voxels per warp block
     static constexpr int BZ = 2 * BD;                          // brick depth
     static constexpr int FW = ADJ ? 24 : (BD == 8 ? 20 : 16);  // footprint width and height
