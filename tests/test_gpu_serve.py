@@ -105,3 +105,21 @@ def test_admission_by_footprint(cuda):
         # the server keeps serving
         out, _ = srv.wait(srv.submit(vid, "forward", axes[:5]))
         assert out.shape == (5, 24, 24) and np.all(np.isfinite(out))
+
+
+def test_large_volume_equals_plain_path(cuda, gglib):
+    """A 256^3 volume (CAS images of 512^2: the serving loop's back projection
+    with 8-deep warp blocks and one brick group per CTA): a back and a forward
+    request equal the plain gridder calls within relative L2 1e-6."""
+    from multigpugridder_gb300.serve import Server
+
+    N = 256
+    v = O.blob_volume(N, 40, seed=71).astype(np.float32)
+    axes = O.quaternion_axes(5, 72).astype(np.float32)
+    imgs = np.random.default_rng(73).standard_normal((len(axes), N, N)).astype(np.float32)
+    with Server(lanes=2) as srv:
+        vid = srv.add_volume(v)
+        back = srv.wait(srv.submit(vid, "back", axes, imgs))[0].copy()
+        fwd = srv.wait(srv.submit(vid, "forward", axes))[0].copy()
+    assert O.rel_l2(back, _plain(gglib, v, "back", axes, imgs)) < 1e-6
+    assert O.rel_l2(fwd, _plain(gglib, v, "forward", axes, None)) < 1e-6
