@@ -112,11 +112,13 @@ def test_back_kernel_other_tables_bit_exact(cuda, gglib, kind):
     assert np.array_equal(vol.cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("N", [21, 50, 100])
+@pytest.mark.parametrize("N", [2, 4, 6, 21, 50, 100])
 def test_back_kernel_other_sizes_bit_exact(cuda, gglib, N):
-    """Volume edges whose CAS images are not a multiple of 4 wide (M = 42:
-    footprints staged pixel by pixel), and brick grids that do not divide the
-    CAS volume (V = 48, 106, 206): equal to the oracle bit for bit."""
+    """Tiny volumes (CAS images of 4-12 pixels, narrower than a footprint,
+    bricks that overhang the whole volume), volume edges whose CAS images are
+    not a multiple of 4 wide (M = 42: footprints staged pixel by pixel), and
+    brick grids that do not divide the CAS volume (V = 48, 106, 206): equal to
+    the oracle bit for bit."""
     import torch
 
     p = O.Params(N)
