@@ -10,8 +10,8 @@
   reads the sources where they lie and writes only the compiled device code.
   The cubins hold GPU code only, so they run on any host architecture; the
   runner in ``oracle/ref_kernels.py`` loads them through the CUDA driver API.
-  It is skipped when the reference checkout is absent (the GPU machine uses the
-  cubins built here).
+  It is skipped when the reference checkout is absent; a machine without the
+  checkout uses cubins built where it was present.
 """
 import os
 import shutil
