@@ -718,7 +718,9 @@ struct alignas(16) BpDirMeta {
 // << 8) in direction order, run 32 at a time, so that rounds are full across
 // directions.  NB footprint buffers per warp: 2 where shared memory allows
 // (a direction's footprint is staged while the previous direction's last
-// voxels still wait in the queue), else 1 (the queue is run empty first).
+// voxels still wait in the queue); else 1, and each direction's active voxels
+// run at once from the same array (a plain list, no queue): queue rounds with
+// one buffer measured slower (per-lane direction records, spills).
 template <bool ADJ, bool DW, bool DEEP>
 struct BpQueue {
     static constexpr int NB = (!ADJ && !DW && !DEEP) ? 2 : 1;
