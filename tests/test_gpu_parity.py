@@ -57,6 +57,31 @@ def test_forward_kernel_matches_oracle(cuda, gglib, N):
     assert np.all(got[ref == 0] == 0)  # outside the mask
 
 
+@pytest.mark.parametrize("N", [2, 4, 6, 21, 50, 100])
+def test_forward_kernel_other_sizes(cuda, gglib, N):
+    """The forward projection at tiny volume edges (tap windows that leave the
+    CAS volume: the reference's linear-index rule), at an odd edge (M = 42) and
+    at edges whose CAS images are not a multiple of the 16-pixel tile: within
+    the FP32 parity bound, and exactly zero outside the mask."""
+    import torch
+
+    p = O.Params(N)
+    rng = np.random.default_rng(400 + N)
+    cas = rng.standard_normal((p.V,) * 3).astype(np.float32)
+    axes = test_axes(6, seed=N + 7)
+    ref = O.fp_ref_f32(cas, axes, p.M, p.mask_radius, p.ker)
+    out = torch.full((len(axes), p.M, p.M), float("nan"), device=cuda)
+    d_cas, d_ker, d_axes = to_dev(cas, cuda), to_dev(p.ker, cuda), to_dev(axes, cuda)
+    rc = gglib.gg_forward_project_kernel(dptr(d_cas), dptr(out), dptr(d_ker), dptr(d_axes), 2.0, len(axes), p.V, p.M,
+                                         3, p.mask_radius, p.ker.size, None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert np.all(np.isfinite(got))
+    assert O.rel_l2(got, ref) < TOL
+    assert np.all(got[ref == 0] == 0)
+
+
 @pytest.mark.parametrize("N", [16, 32, 64])
 def test_back_kernel_matches_oracle(cuda, gglib, N):
     import torch
