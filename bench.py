@@ -274,7 +274,8 @@ def run_gb300(args):
     achieved = bpu[dom] * units_per_launch / (tot_ms / max(cnt, 1) / 1e3) / 1e9
     peaks = {}
     try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
     except (OSError, ValueError):
         pass
     peak = peaks.get("hbm_gbs") or 6800.0

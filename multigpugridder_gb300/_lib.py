@@ -129,7 +129,8 @@ class GridderError(RuntimeError):
 
 def declared_symbols():
     """Function names declared in include/gg_gridder.h."""
-    txt = open(HEADER).read()
+    with open(HEADER) as f:
+        txt = f.read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     return sorted(set(re.findall(r"\b(gg_[a-z0-9_]+)\s*\(", txt)))
 

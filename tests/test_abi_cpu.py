@@ -115,7 +115,8 @@ def test_compat_header_names_are_exported(L):
     import re
 
     path = os.path.join(ROOT, "include", "gg_compat.h")
-    txt = re.sub(r"/\*.*?\*/", "", open(path).read(), flags=re.S)
+    with open(path) as f:
+        txt = re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
     names = sorted(set(re.findall(r"\b([A-Z][A-Za-z_]+)\s*\(", txt)))
     want = {"Gridder_new", "SetNumberGPUs", "SetNumberStreams", "SetVolume", "GetVolume", "ResetVolume", "SetImages",
             "GetImages", "SetAxes", "SetImgSize", "SetMaskRadius", "Forward_Project", "Back_Project"}

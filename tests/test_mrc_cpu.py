@@ -16,7 +16,8 @@ def test_round_trip_volume_and_header(tmp_path):
     write_mrc(p, vol, voxel_size=1.5)
     got, vs = read_mrc(p)
     assert np.array_equal(got, vol) and vs == 1.5
-    head = open(p, "rb").read(1024)
+    with open(p, "rb") as f:
+        head = f.read(1024)
     assert struct.unpack("<4i", head[:16]) == (4, 5, 6, 2)          # NX NY NZ MODE, x fastest
     assert struct.unpack("<3i", head[28:40]) == (4, 5, 6)           # MX MY MZ
     assert struct.unpack("<3f", head[40:52]) == (6.0, 7.5, 9.0)     # cell (Å)

@@ -206,7 +206,7 @@ def test_model_get_volume_c2r():
                     r1 = cas[k + b, j + b, i + b]
                     r2 = cas[M - k + b, M - j + b, M - i + b]
                     spec[w, v, u] = 0.5 * (r1 + r2) + 0.5j * (r1 - r2)
-    y = np.fft.irfftn(spec, s=(M, M, M)) * M ** 3
+    y = np.fft.irfftn(spec, s=(M, M, M), axes=(0, 1, 2)) * M ** 3
     pc = O.precomp(M)
     ob = M // 2 - N // 2
     idx = _shift(np.arange(N) + ob, M)
