@@ -58,15 +58,15 @@ __device__ __forceinline__ void load_table(float *sker, const float *ker, int ke
     for (int t = threadIdx.x; t < kerSize; t += blockDim.x) sker[t] = __ldg(ker + t);
 }
 
+// Device attributes, read once (thread-safe static initialisation).
 static int num_sms()
 {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    static const int sms = [] {
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        return v > 0 ? v : 1;
+    }();
     return sms;
 }
 
@@ -630,13 +630,12 @@ __device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fb
 
 static int max_dyn_smem()
 {
-    static int bytes = 0;
-    if (bytes == 0) {
-        int dev = 0;
+    static const int bytes = [] {
+        int dev = 0, v = 0;
         cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&bytes, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (bytes <= 0) bytes = 48 * 1024;
-    }
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        return v > 0 ? v : 48 * 1024;
+    }();
     return bytes;
 }
 
