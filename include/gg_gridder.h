@@ -213,10 +213,11 @@ int gg_back_project_adjoint_kernel(float *d_cas_volume, const float *d_cas_image
    not start at zero; the scratch must be zero when the back projection
    starts, and the call zeroes it itself on `stream` first.  All calls on one
    device share the scratch: calls that overlap (different streams or threads
-   with no ordering between them) race on it.  The first call on each device
-   looks up the scratch address (cudaGetSymbolAddress, which may load the
-   library's module onto the device) and should come before any stream
-   capture. */
+   with no ordering between them) race on it.  Every call looks up the
+   scratch address in the current context (cudaGetSymbolAddress, no cache:
+   a cudaDeviceReset or a second context on the device would leave a cached
+   address stale).  The first call in a context may load the library's
+   module onto the device, so it should come before any stream capture. */
 int gg_back_project_normalized_noalloc(float *d_cas_volume_out, const float *d_cas_images, const float *d_kb_table,
                                        const float *d_axes, float ker_hwidth, int n_axes, int cas_vol_size,
                                        int cas_img_size, int mask_radius, int kb_table_size, void *stream);

@@ -1291,7 +1291,7 @@ extern "C" int gg_forward_project_adjoint(gg_gridder *h, const float *axes, int 
 
 // ---- stateless kernel entry points ------------------------------------------
 
-static int check_kernel_args(float ker_hwidth, int n_axes, int V, int M, int mask_radius, int kb_size)
+int gg::check_kernel_args(float ker_hwidth, int n_axes, int V, int M, int mask_radius, int kb_size)
 {
     if ((int)roundf(ker_hwidth) != 2 || ker_hwidth != 2.0f) {
         g_global_err = "only kerHWidth = 2 is supported (the reference fixes it, AbstractGridder.cpp:10)";

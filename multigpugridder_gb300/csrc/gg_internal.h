@@ -169,6 +169,11 @@ void count_launches(long long n);
 // Sets the calling thread's message returned by gg_global_error().
 void set_global_error(const char *msg);
 
+// Argument checks shared by the stateless kernel entry points: kerHWidth 2,
+// sizes positive, a KB table of 3..kMaxKerSizeHost entries.  Returns GG_OK or
+// GG_ERR_INVALID_ARG with the message set for gg_global_error().
+int check_kernel_args(float ker_hwidth, int n_axes, int V, int M, int mask_radius, int kb_size);
+
 // ---- a gridder's resident state, for the serving loop (gg_api.cu) ---------
 struct GridderView {
     int device, N, M, V;

@@ -14,15 +14,12 @@
 // (16 MiB), so cas_vol_size^3 <= 4,194,304 (cas_vol_size <= 161).  Calls that
 // overlap on one device share it and race; callers order them (one stream, or
 // events between streams).
-#include <mutex>
-
 #include "gg_internal.h"
 #include "../../include/gg_gridder.h"
 
 namespace gg {
 
 constexpr size_t kNoAllocMaxVoxels = (size_t)4 << 20; // 16 MiB of FP32
-constexpr int kNoAllocMaxDevices = 64;
 
 // Plane density of the current call.  Only its first V^3 floats are used;
 // they must be zero when the fused kernel starts, and each call zeroes them
@@ -31,36 +28,24 @@ static __device__ __align__(256) float g_noalloc_plane_density[kNoAllocMaxVoxels
 
 namespace {
 
-std::mutex g_noalloc_mu;
-float *g_noalloc_scratch[kNoAllocMaxDevices]; // device address per device ordinal
-
-// Device address of the scratch on the current device, looked up once per
-// device.  The lookup may load this library's module onto the device, so the
-// first call on a device does set-up work.
+// Device address of the scratch array in the current context.  In host code
+// the array's name stands for a host-side shadow, not device memory, so the
+// address is looked up with cudaGetSymbolAddress.  The lookup is made on
+// every call and not cached: the address belongs to the context the
+// library's module is loaded in, and a cudaDeviceReset (a MATLAB
+// reset(gpuDevice), say) or another context on the same device makes a
+// cached address stale.  The lookup allocates nothing; the first one in a
+// context may load the module onto the device.
 int noalloc_scratch(float **out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        set_global_error(cudaGetErrorString(e));
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_plane_density);
+    if (e != cudaSuccess || !p) {
+        set_global_error(e != cudaSuccess ? cudaGetErrorString(e)
+                                          : "cudaGetSymbolAddress returned no address for the scratch array");
         return GG_ERR_CUDA;
     }
-    if (dev < 0 || dev >= kNoAllocMaxDevices) {
-        set_global_error("device ordinal out of range for the no-allocation scratch table");
-        return GG_ERR_INVALID_ARG;
-    }
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_scratch[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_plane_density);
-        if (e != cudaSuccess || !p) {
-            set_global_error(e != cudaSuccess ? cudaGetErrorString(e)
-                                              : "cudaGetSymbolAddress returned no address for the scratch array");
-            return GG_ERR_CUDA;
-        }
-        g_noalloc_scratch[dev] = (float *)p;
-    }
-    *out = g_noalloc_scratch[dev];
+    *out = (float *)p;
     return GG_OK;
 }
 
@@ -74,15 +59,8 @@ extern "C" int gg_back_project_normalized_noalloc(float *d_cas_volume_out, const
                                                   int n_axes, int cas_vol_size, int cas_img_size, int mask_radius,
                                                   int kb_table_size, void *stream)
 {
-    if (ker_hwidth != 2.0f) {
-        set_global_error("only kerHWidth = 2 is supported (the reference fixes it, AbstractGridder.cpp:10)");
-        return GG_ERR_INVALID_ARG;
-    }
-    if (n_axes < 0 || cas_vol_size <= 0 || cas_img_size <= 0 || mask_radius < 0 || kb_table_size < 3 ||
-        kb_table_size > kMaxKerSizeHost) {
-        set_global_error("invalid sizes");
-        return GG_ERR_INVALID_ARG;
-    }
+    int rc = check_kernel_args(ker_hwidth, n_axes, cas_vol_size, cas_img_size, mask_radius, kb_table_size);
+    if (rc != GG_OK) return rc;
     const size_t V3 = (size_t)cas_vol_size * cas_vol_size * cas_vol_size;
     if (V3 > kNoAllocMaxVoxels) {
         set_global_error("gg_back_project_normalized_noalloc: cas_vol_size^3 exceeds the fixed plane-density "
@@ -94,7 +72,7 @@ extern "C" int gg_back_project_normalized_noalloc(float *d_cas_volume_out, const
         return GG_ERR_INVALID_ARG;
     }
     float *pd = nullptr;
-    int rc = noalloc_scratch(&pd);
+    rc = noalloc_scratch(&pd);
     if (rc != GG_OK) return rc;
 
     const cudaStream_t s = (cudaStream_t)stream;

@@ -8,6 +8,7 @@
 // src/Projection/gpuBackProject.cu): x fastest, CAS-volume centre V/2, image
 // centre M/2, nearest-index lookup into the KB table, int mask radius.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -58,16 +59,36 @@ __device__ __forceinline__ void load_table(float *sker, const float *ker, int ke
     for (int t = threadIdx.x; t < kerSize; t += blockDim.x) sker[t] = __ldg(ker + t);
 }
 
-// Device attributes, read once (thread-safe static initialisation).
+// An attribute of the current device, cached per device ordinal (a process
+// may drive GPUs of different kinds).  cache[] starts at zero; a racing
+// first read stores the same value twice.
+constexpr int kAttrCacheDevices = 64;
+
+static int device_attr(cudaDeviceAttr attr, std::atomic<int> *cache, int fallback)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return fallback;
+    }
+    const bool cached = dev >= 0 && dev < kAttrCacheDevices;
+    if (cached) {
+        const int v = cache[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, attr, dev) != cudaSuccess || v <= 0) {
+        cudaGetLastError();
+        return fallback;
+    }
+    if (cached) cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
+
 static int num_sms()
 {
-    static const int sms = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-        return v > 0 ? v : 1;
-    }();
-    return sms;
+    static std::atomic<int> cache[kAttrCacheDevices];
+    return device_attr(cudaDevAttrMultiProcessorCount, cache, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -630,13 +651,8 @@ __device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fb
 
 static int max_dyn_smem()
 {
-    static const int bytes = [] {
-        int dev = 0, v = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        return v > 0 ? v : 48 * 1024;
-    }();
-    return bytes;
+    static std::atomic<int> cache[kAttrCacheDevices];
+    return device_attr(cudaDevAttrMaxSharedMemoryPerBlockOptin, cache, 48 * 1024);
 }
 
 // The table layout for kerSize entries beside other_bytes of shared memory:

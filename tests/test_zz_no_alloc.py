@@ -84,7 +84,7 @@ def test_noalloc_leaves_free_device_memory_unchanged(cuda, gglib):
     ker = _dev(p.ker, cuda)
     img, axes = _case(p, 30, 700, cuda)
     out = torch.empty((p.V,) * 3, device=cuda)
-    _noalloc(gglib, out, img, ker, axes, p)  # the first call on the device does the set-up
+    _noalloc(gglib, out, img, ker, axes, p)  # the first call in the context may load the module
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info()[0]
     for _ in range(2):
