@@ -50,19 +50,24 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=1024,
                     help="directions timed by the CPU baseline / reference arm per step (one core: 1/8 of it)")
-    ap.add_argument("--serve-seconds", type=float, default=2.0,
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
                     help="arrival window of the serving workload (0: skip it)")
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="offered requests/s (Poisson)")
     ap.add_argument("--serve-lanes", type=int, default=8)
     ap.add_argument("--serve-closed", type=int, default=200,
                     help="requests in the closed-loop served vs sequential plain-path comparison")
+    ap.add_argument("--serve-repeats", type=int, default=5, help="repeats of the closed-loop comparison")
     ap.add_argument("--no-precision", action="store_true", help="skip the 256^3 storage-precision comparison")
     ap.add_argument("--no-autograd", action="store_true", help="skip the gradient-descent timing")
     ap.add_argument("--no-ctf", action="store_true", help="skip the CTF-corrected reconstruction timing")
     return ap.parse_args()
 
 
-def workload(args):
+def workload(args, rank=0, world=1):
+    """The volume and this rank's directions.  One GPU: the 100 x 100 grid
+    (in-plane angle 30 degrees).  World W > 1 (weak scaling): W x 10,000
+    directions, shard r being the same grid turned in-plane by 360 r / W
+    degrees more."""
     from multigpugridder_gb300 import synthetic
 
     N = args.size
@@ -70,10 +75,31 @@ def workload(args):
     vol = synthetic.blob_volume(N, n_blobs, seed=2)
     side = int(round(args.directions ** 0.5))
     if side * side == args.directions:
-        axes = synthetic.grid_axes(side, side).astype(np.float32)
+        axes = synthetic.grid_axes(side, side, psi_deg=30.0 + 360.0 * rank / world).astype(np.float32)
     else:
-        axes = synthetic.quaternion_axes(args.directions, seed=2).astype(np.float32)
+        axes = synthetic.quaternion_axes(args.directions, seed=2 + rank).astype(np.float32)
     return vol, axes
+
+
+FLUSH_BYTES = 512 << 20  # untimed write between steps: 4x the 126 MB L2
+
+
+def sizes(args):
+    """(N, M, V) of the workload: interpFactor 2, extra padding 3."""
+    N = args.size
+    return N, 2 * N, 2 * N + 6
+
+
+def bench_config(args, world):
+    """The `config` both arms print (the same dict, so the two lines compare)."""
+    N, M, V = sizes(args)
+    return {"workload": "%d^3 volume, interpFactor 2 (CAS volume %d^3, CAS images %d^2), %d directions: "
+                        "setVolume + forwardProject + reconstructVol" % (N, V, M, args.directions),
+            "N": N, "M": M, "V": V, "directions": args.directions, "batch": args.batch,
+            "precision": args.precision,
+            "parallelism": ("orientation shards x%d, one all-reduce" % world) if world > 1 else "single",
+            "l2": "inputs larger than L2 (%d images = %d MB per step) and an untimed %d MB write between steps"
+                  % (args.directions, args.directions * N * N * 4 >> 20, FLUSH_BYTES >> 20)}
 
 
 def p_in(M, R):
@@ -138,42 +164,55 @@ class ClockSampler:
 
 
 def cpu_baseline(vol, axes, args, threads=None, sample=None):
+    """One CPU step of the restated reference path on a bounded sample of the
+    directions; returns (pairs/s measured on the sample, details, S)."""
     from oracle import cpu_path, oracle as O
 
     p = O.Params(args.size)
     S = min(sample or args.cpu_sample, len(axes))
     idx = np.linspace(0, len(axes) - 1, S).round().astype(int)
-    t_step, det = cpu_path.time_step(vol, axes[idx], p, len(axes), threads=threads)
-    return len(axes) / t_step, det, S
+    t, det = cpu_path.time_step(vol, axes[idx], p, len(axes), threads=threads)
+    det["t_step_s"] = t
+    return S / t, det, S
 
 
 def run_reference(args):
+    """The reference's gridding path on the host cores (the restatement in
+    oracle/: the reference has no CPU implementation of it).  Each step is
+    setVolume + forwardProject + reconstructVol of a bounded sample of the
+    workload's directions (evenly spaced); value = sample directions / the
+    measured step time.  The full-workload step it stands for is extrapolated
+    and reported apart."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     vol, axes = workload(args)
-    from oracle import cpu_path
-
-    vals = []
-    det = None
+    times, dets = [], []
+    S = 0
     for s in range(args.warmup + args.steps):
-        v, det, S = cpu_baseline(vol, axes, args)
+        _, det, S = cpu_baseline(vol, axes, args)
         if s >= args.warmup:
-            vals.append(v)
-    value = statistics.median(vals)
+            times.append(det["t_step_s"])
+            dets.append(det)
+    t_step = statistics.mean(times)
+    value = S / t_step
+    det = dets[-1]
+    t_full = statistics.mean(d["t_step_extrapolated_s"] for d in dets)
     cores = det["threads"]
-    sample = ("%d of the %d directions (evenly spaced) through the restated reference path: FP32 CAS prep "
-              "(scipy.fft), forward-projection kernel, 2-D FFTs, back projection and plane density "
-              "(gg_oracle.c, OpenMP), getVol; step time extrapolated as t_fixed + D/S * t_sample"
-              % (S, len(axes)))
-    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": len(axes) / value * 1e3,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+    sample = ("each step: %d of the %d directions (evenly spaced) through the restated reference path: FP32 CAS "
+              "prep (scipy.fft), forward-projection kernel, 2-D FFTs, back projection and plane density "
+              "(gg_oracle.c, OpenMP), getVol; value = %d / measured step time" % (S, len(axes), S))
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
            "data": "synthetic (seeded Gaussian-blob volume, 100x100 direction grid)",
-           "config": {"workload": "128^3 volume, interpFactor 2 (CAS volume 262^3), 10,000 directions, "
-                                  "forwardProject + reconstructVol", "N": args.size, "directions": len(axes)},
+           "config": bench_config(args, world),
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "directions_per_step": S,
+           "full_step_extrapolated": {"ms": t_full * 1e3, "value": len(axes) / t_full, "unit": UNIT,
+                                      "how": "t_fixed + D/S * t_sample, D = %d" % len(axes)},
            "details": det}
     print(json.dumps(out), flush=True)
 
@@ -194,7 +233,7 @@ def run_gb300(args):
     dev = torch.device("cuda", local)
     L = lib()
 
-    vol, axes = workload(args)
+    vol, axes = workload(args, rank, world)
     n = len(axes)
     N = args.size
     g = gg.MultiGPUGridder(N, n, 2.0, GPUs=[local], MaxAxesToAllocate=args.batch, precision=args.precision)
@@ -206,8 +245,8 @@ def run_gb300(args):
     d_axes = torch.from_numpy(axes).to(dev)
     d_imgs = torch.empty((n, N, N), dtype=torch.float32, device=dev)
     d_out = torch.empty((N, N, N), dtype=torch.float32, device=dev)
-    l2 = torch.cuda.get_device_properties(dev).L2_cache_size if hasattr(torch.cuda.get_device_properties(dev), "L2_cache_size") else 128 << 20
-    flush = torch.empty(max(4 * l2, 512 << 20) // 4, dtype=torch.float32, device=dev)
+    d_sums = torch.empty((2, V, V, V), dtype=torch.float32, device=dev) if world > 1 else None
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     def vp(t):
         return ctypes.c_void_p(t.data_ptr())
@@ -215,7 +254,14 @@ def run_gb300(args):
     def step():
         check(L.gg_set_volume_dev(h, vp(d_vol), sp), h)
         check(L.gg_forward_project_dev(h, vp(d_axes), n, vp(d_imgs), None, sp), h)
-        check(L.gg_reconstruct_volume_dev(h, vp(d_axes), n, vp(d_imgs), vp(d_out), sp), h)
+        if world == 1:
+            check(L.gg_reconstruct_volume_dev(h, vp(d_axes), n, vp(d_imgs), vp(d_out), sp), h)
+        else:
+            # the reference's split (MultiGPUGridder.cpp:37-96, 376-411): this rank's
+            # sums, one all-reduce of CAS volume + plane density, division and getVol
+            check(L.gg_back_project_sums_dev(h, vp(d_axes), n, vp(d_imgs), vp(d_sums), sp), h)
+            dist.all_reduce(d_sums)
+            check(L.gg_volume_from_sums_dev(h, vp(d_sums), vp(d_out), sp), h)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -292,24 +338,30 @@ def run_gb300(args):
 
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(args, g, vol, axes, world)
+        e2e = run_e2e(args, g, vol, axes, world, dev)
 
     base = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, det, S = cpu_baseline(vol, axes, args)
         base = {"value": v, "unit": UNIT, "cores": det["threads"], "kind": "port",
-                "sample": "%d of %d directions timed, step extrapolated (t_fixed + D/S * t_sample)" % (S, n)}
+                "sample": "one step of setVolume + forwardProject + reconstructVol on %d of the %d directions "
+                          "(evenly spaced); value = %d / measured step time" % (S, n, S),
+                "full_step_extrapolated": n / det["t_step_extrapolated_s"]}
         # the same port on one core, on a smaller sample
         v1, _, S1 = cpu_baseline(vol, axes, args, threads=1, sample=max(1, args.cpu_sample // 8))
         base["one_core"] = {"value": v1, "cores": 1,
-                            "sample": "%d of %d directions timed on one thread, step extrapolated" % (S1, n)}
+                            "sample": "one step on %d of %d directions, one thread" % (S1, n)}
 
     g.close()
     serve = prec = grad = ctf = None
     if rank == 0 and world == 1 and args.serve_seconds > 0:
         serve = run_serve(args)
     if rank == 0 and world == 1 and not args.no_precision and args.size == 128:
-        prec = run_precision(args)
+        prec, keep = run_precision(args)
+        if not args.no_cpu_baseline:
+            # CPU leg: the FP64 oracle as the checker of the reduced-precision results
+            prec["vs_f64"] = check_precision_vs_f64(keep)
+        del keep
     if rank == 0 and world == 1 and not args.no_autograd and args.size == 128:
         grad = run_autograd(args)
     if rank == 0 and world == 1 and not args.no_ctf:
@@ -319,12 +371,7 @@ def run_gb300(args):
                "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": args.precision,
                "data": "synthetic (seeded Gaussian-blob volume, 100x100 direction grid)",
-               "config": {"workload": "128^3 volume, interpFactor 2 (CAS volume 262^3, CAS images 256^2), "
-                                      "10,000 directions: setVolume + forwardProject + reconstructVol",
-                          "N": N, "M": M, "V": V, "directions": n, "batch": args.batch,
-                          "precision": args.precision, "parallelism": "replicas" if world > 1 else "single",
-                          "l2": "inputs larger than L2 (10,000 images = %d MB per step) and an untimed %d MB "
-                                "write between steps" % (n * N * N * 4 >> 20, flush.numel() * 4 >> 20)},
+               "config": bench_config(args, world),
                "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
                "clocks": clk, "step_ms": ms_steps, "serve": serve, "precision": prec, "autograd": grad,
                "ctf": ctf}
@@ -368,11 +415,10 @@ def run_serve(args):
     L = lib()
     offered = serve_schedule(args.serve_seconds, args.serve_rate)
     closed = offered[:args.serve_closed]
-    axes = {}
-    for sched in (offered,):
-        for _, _, _, n, seed in sched:
-            if seed not in axes:
-                axes[seed] = synthetic.quaternion_axes(n, seed).astype(np.float32)
+    # request k takes the first n directions of direction set k mod 64 (4,096
+    # random-quaternion directions each): a bounded host footprint for any run length
+    pool = [synthetic.quaternion_axes(4096, 1000 + k).astype(np.float32) for k in range(64)]
+    axes = {seed: pool[(seed - 1000) % len(pool)] for _, _, _, _, seed in offered}
     vols = [synthetic.blob_volume(N, b, seed=50 + i) for i, (N, b) in enumerate(zip(SERVE_SIZES, SERVE_BLOBS))]
     srv = Server(lanes=args.serve_lanes)
     vids = [srv.add_volume(v) for v in vols]
@@ -420,11 +466,13 @@ def run_serve(args):
     # warm the lanes, then the closed loop: all requests queued at once
     for h in [submit(si, op, min(n, 64), seed) for _, si, op, n, seed in closed[:16]]:
         srv.wait(h)
-    t0 = time.perf_counter()
-    hs = [submit(si, op, n, seed) for _, si, op, n, seed in closed]
-    for h in hs:
-        srv.wait(h)
-    served_closed = len(closed) / (time.perf_counter() - t0)
+
+    def served_once():
+        t0 = time.perf_counter()
+        hs = [submit(si, op, n, seed) for _, si, op, n, seed in closed]
+        for h in hs:
+            srv.wait(h)
+        return len(closed) / (time.perf_counter() - t0)
     # the same requests one at a time through the plain gridder calls
     grids = []
     for v, (N, M, V) in zip(vols, sizes):
@@ -448,10 +496,18 @@ def run_serve(args):
 
     for _, si, op, n, seed in closed[:16]:
         plain(si, op, min(n, 64), seed)
-    t0 = time.perf_counter()
-    for _, si, op, n, seed in closed:
-        plain(si, op, n, seed)
-    seq_closed = len(closed) / (time.perf_counter() - t0)
+
+    def sequential_once():
+        t0 = time.perf_counter()
+        for _, si, op, n, seed in closed:
+            plain(si, op, n, seed)
+        return len(closed) / (time.perf_counter() - t0)
+
+    # alternate the two arms so that drifts of the shared GPU hit both alike
+    served_runs, seq_runs = [], []
+    for _ in range(max(1, args.serve_repeats)):
+        served_runs.append(served_once())
+        seq_runs.append(sequential_once())
     for h in grids:
         L.gg_destroy(h)
 
@@ -465,34 +521,52 @@ def run_serve(args):
                         "log-uniform 16-4096 (random quaternions); back requests return the CAS volume"
                         % (args.serve_rate, args.serve_seconds),
             "lanes": args.serve_lanes, "offered": res_offered, "at_70pct_capacity": res_70,
-            "closed_loop": {"requests": len(closed), "served_rps": served_closed, "sequential_plain_rps": seq_closed,
-                            "speedup": served_closed / seq_closed}}
+            "closed_loop": {"requests": len(closed), "repeats": len(served_runs),
+                            "served_rps": statistics.median(served_runs),
+                            "sequential_plain_rps": statistics.median(seq_runs),
+                            "speedup": statistics.median(a / b for a, b in zip(served_runs, seq_runs)),
+                            "served_rps_runs": served_runs, "sequential_plain_rps_runs": seq_runs}}
 
 
 # ---- storage precision at 256^3 ------------------------------------------------
+PREC_SUBSET = 64  # directions of the 5,000 compared against the FP64 oracle
+
+
+def precision_workload():
+    from multigpugridder_gb300 import synthetic
+
+    N, n = 256, 5000
+    vol = synthetic.blob_volume(N, 400, seed=3)
+    axes = synthetic.quaternion_axes(n, seed=3).astype(np.float32)
+    sub = np.linspace(0, n - 1, PREC_SUBSET).round().astype(int)
+    return N, n, vol, axes, sub
+
+
 def run_precision(args):
     """256^3 Gaussian-blob volume (400 blobs), interpFactor 2 (CAS volume 518^3),
     5,000 random-quaternion directions: setVolume + forwardProject +
     reconstructVol with FP32, BF16 and FP16 storage (FP32 accumulation).
     Reports pairs/s per storage type and the relative L2 of the images and the
-    reconstruction against the FP32 path (the FP64 oracle comparison runs in
-    tests/test_gpu_precision.py at sizes the CPU finishes)."""
+    reconstruction against the FP32 path.  It also keeps, per storage type,
+    the images of a fixed subset of 64 directions and a reconstructVol of the
+    FP32 path's images of those directions, for the FP64 comparison that the
+    CPU leg makes (check_precision_vs_f64)."""
     import torch
 
     import multigpugridder_gb300 as gg
-    from multigpugridder_gb300 import synthetic
     from multigpugridder_gb300._lib import check, lib
 
     L = lib()
-    N, n = 256, 5000
-    vol = synthetic.blob_volume(N, 400, seed=3)
-    axes = synthetic.quaternion_axes(n, seed=3).astype(np.float32)
+    N, n, vol, axes, sub = precision_workload()
     dev = torch.device("cuda", torch.cuda.current_device())
     d_vol = torch.from_numpy(vol).to(dev)
     d_axes = torch.from_numpy(axes).to(dev)
+    d_sub = torch.from_numpy(sub).to(dev)
+    d_sub_axes = d_axes[d_sub].contiguous()
     stream = torch.cuda.Stream(device=dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
-    out, ref = {}, {}
+    out, ref, keep = {}, {}, {}
+    sub_imgs_f32 = None
 
     def vp(t):
         return ctypes.c_void_p(t.data_ptr())
@@ -522,16 +596,48 @@ def run_precision(args):
         res = {"pairs_per_s": n / (ms / 1e3), "ms_per_step": ms}
         if prec == "f32":
             ref = {"images": imgs.clone(), "rec": rec.clone()}
+            sub_imgs_f32 = imgs[d_sub].contiguous()
         else:
             for k, t in (("images", imgs), ("rec", rec)):
                 res["rel_l2_%s_vs_f32" % k] = float(torch.linalg.vector_norm((t - ref[k]).double())
                                                     / torch.linalg.vector_norm(ref[k].double()))
+        # reconstructVol of the subset's FP32 images (the same input for every storage type)
+        rec_sub = torch.empty((N, N, N), dtype=torch.float32, device=dev)
+        with torch.cuda.stream(stream):
+            check(L.gg_reconstruct_volume_dev(h, vp(d_sub_axes), len(sub), vp(sub_imgs_f32), vp(rec_sub), sp), h)
+        torch.cuda.synchronize()
+        keep[prec] = {"images": imgs[d_sub].cpu().numpy(), "rec": rec_sub.cpu().numpy()}
         out[prec] = res
         g.close()
-        del imgs, rec
+        del imgs, rec, rec_sub
+    keep["input_images"] = sub_imgs_f32.cpu().numpy()
     return {"workload": "256^3 volume (400 blobs), interpFactor 2 (CAS volume 518^3), 5,000 random-quaternion "
                         "directions: setVolume + forwardProject + reconstructVol, storage f32/bf16/f16 (volume and "
-                        "CAS images) and bf16_vol (BF16 volume, FP32 CAS images), FP32 accumulation", "results": out}
+                        "CAS images) and bf16_vol (BF16 volume, FP32 CAS images), FP32 accumulation",
+            "results": out}, keep
+
+
+def check_precision_vs_f64(keep):
+    """FP64 oracle references for the precision leg (part of the CPU leg):
+    forwardProject of the 64-direction subset and reconstructVol of the FP32
+    path's images of those directions, both in FP64 on the host; returns
+    rel-L2 of each storage type's images and reconstruction against them."""
+    from oracle import oracle as O
+
+    N, n, vol, axes, sub = precision_workload()
+    p = O.Params(N)
+    t0 = time.perf_counter()
+    ref_imgs, _ = O.forward_project(vol, axes[sub], p, precision="f64")
+    ref_rec, _, _ = O.reconstruct_vol(keep["input_images"].astype(np.float64), axes[sub], p, precision="f64")
+    res = {"subset": "%d of the %d directions (evenly spaced); images: forwardProject; rec: reconstructVol of the "
+                     "FP32 path's images of those directions" % (len(sub), n),
+           "oracle_seconds": time.perf_counter() - t0}
+    for prec, k in keep.items():
+        if prec == "input_images":
+            continue
+        res[prec] = {"rel_l2_images_vs_f64": O.rel_l2(k["images"], ref_imgs),
+                     "rel_l2_rec_vs_f64": O.rel_l2(k["rec"], ref_rec)}
+    return res
 
 
 # ---- differentiation -----------------------------------------------------------
@@ -539,30 +645,49 @@ def run_autograd(args):
     """torch FP32 volume 128^3 (requires_grad, Gaussian-blob init), interpFactor
     2, batches of 4,096 random directions, loss ||P(V) - Y||^2 with
     Y = P(V_true) + Gaussian noise at SNR 0.1, backward through the exact
-    adjoint; 20 gradient-descent iterations timed."""
+    adjoint; 20 gradient-descent iterations timed, cycling over 4 batches.
+
+    Step size 1 / L with L = 2 * 1.1 * lambda_max(P^T P), lambda_max from 15
+    power iterations on the first batch (untimed): for a quadratic loss a
+    step of 1 / L never increases it.  The noise floor is sum ||noise_k||^2
+    over the 4 batches; `excess_removed` is the fraction of the loss above
+    that floor that the 20 iterations remove (last cycle against first)."""
     import torch
 
     from multigpugridder_gb300 import synthetic
     from multigpugridder_gb300.autograd import ForwardProjector
 
-    N, B, iters = 128, 4096, 20
+    N, B, iters, nb = 128, 4096, 20, 4
     dev = torch.device("cuda", torch.cuda.current_device())
     proj = ForwardProjector(N, 2.0, max_batch=B)
     v_true = torch.from_numpy(synthetic.blob_volume(N, 100, seed=4)).to(dev)
     batches = []
-    for k in range(4):
+    floor = 0.0
+    for k in range(nb):
         ax = torch.from_numpy(synthetic.quaternion_axes(B, seed=40 + k).astype(np.float32)).to(dev)
         with torch.no_grad():
             clean = proj.project(v_true, ax)
             sigma = float(torch.sqrt(clean.var() / 0.1))
             gen = torch.Generator(device=dev).manual_seed(400 + k)
-            y = clean + sigma * torch.randn(clean.shape, device=dev, generator=gen)
+            noise = sigma * torch.randn(clean.shape, device=dev, generator=gen)
+            floor += float(torch.sum(noise.double() ** 2))
+            y = clean + noise
         batches.append((ax, y))
+        del clean, noise
+    # largest eigenvalue of P^T P by power iteration
+    with torch.no_grad():
+        x = torch.randn((N,) * 3, device=dev, generator=torch.Generator(device=dev).manual_seed(7))
+        lam = 0.0
+        for _ in range(15):
+            x = x / torch.linalg.vector_norm(x)
+            x = proj.adjoint(proj.project(x, batches[0][0]), batches[0][0])
+            lam = float(torch.linalg.vector_norm(x))
+    lr = 1.0 / (2.0 * 1.1 * lam)
     vol = torch.from_numpy(synthetic.blob_volume(N, 100, seed=41)).to(dev).requires_grad_(True)
-    lr = 1e-9
+    vol0 = vol.detach().clone()
 
     def it(k):
-        ax, y = batches[k % len(batches)]
+        ax, y = batches[k % nb]
         loss = torch.sum((proj.project(vol, ax) - y) ** 2)
         loss.backward()
         with torch.no_grad():
@@ -570,8 +695,11 @@ def run_autograd(args):
             vol.grad = None
         return loss.detach()
 
+    # warm-up on the same iterations, then restart from the initial volume
     for k in range(2):
         it(k)
+    with torch.no_grad():
+        vol.copy_(vol0)
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     losses = []
@@ -581,13 +709,20 @@ def run_autograd(args):
     b.record()
     torch.cuda.synchronize()
     ms = a.elapsed_time(b) / iters
+    with torch.no_grad():
+        err0 = float(torch.linalg.vector_norm(vol0 - v_true) / torch.linalg.vector_norm(v_true))
+        err1 = float(torch.linalg.vector_norm(vol.detach() - v_true) / torch.linalg.vector_norm(v_true))
     proj.close()
-    first = [float(x) for x in losses[:4]]
-    last = [float(x) for x in losses[-4:]]
-    return {"workload": "128^3 FP32 volume, interpFactor 2, batches of 4,096 random directions, loss "
-                        "||P(V) - Y||^2 (Y = P(V_true) + noise at SNR 0.1), 20 gradient-descent iterations",
-            "ms_per_iteration": ms, "directions_per_s": B / (ms / 1e3),
-            "loss_first_cycle": sum(first), "loss_last_cycle": sum(last)}
+    first = sum(float(x) for x in losses[:nb])
+    last = sum(float(x) for x in losses[-nb:])
+    return {"workload": "128^3 FP32 volume, interpFactor 2, batches of 4,096 random directions (4 batches "
+                        "cycled), loss ||P(V) - Y||^2 (Y = P(V_true) + noise at SNR 0.1), 20 gradient-descent "
+                        "iterations, step 1/L from power iteration",
+            "ms_per_iteration": ms, "directions_per_s": B / (ms / 1e3), "step_size": lr,
+            "lambda_max": lam, "loss_first_cycle": first, "loss_last_cycle": last, "noise_floor": floor,
+            "excess_removed": (first - last) / (first - floor) if first > floor else None,
+            "losses": [float(x) for x in losses],
+            "rel_error_to_v_true": {"start": err0, "end": err1}}
 
 
 # ---- CTF application before back projection ------------------------------------
@@ -638,20 +773,33 @@ def run_ctf(args, vol, axes):
     return res
 
 
-def run_e2e(args, g, vol, axes, world):
-    """The same step through the host-pointer ABI with pinned host buffers."""
+def run_e2e(args, g, vol, axes, world, dev):
+    """The same step through the host-pointer ABI with pinned host buffers:
+    volume and axes in, this rank's images out and back in, volume out.  With
+    W > 1 ranks the images go back in as the sums call's device input (one
+    pinned copy) and the step ends with the all-reduce, the division and getVol
+    as in the timed step; time is the max over ranks."""
     import torch
+    import torch.distributed as dist
 
     from multigpugridder_gb300._lib import check, lib
+    from multigpugridder_gb300.sharding import max_over_ranks
 
     L = lib()
     h = g.handle
-    n, N = len(axes), args.size
+    n, N, V = len(axes), args.size, g.V
     h_vol = torch.from_numpy(vol).pin_memory()
     h_axes = torch.from_numpy(axes).pin_memory()
     h_imgs = torch.empty((n, N, N), dtype=torch.float32).pin_memory()
     h_out = torch.empty((N, N, N), dtype=torch.float32).pin_memory()
     dims = (ctypes.c_int * 3)(N, N, N)
+    if world > 1:
+        stream = torch.cuda.Stream(device=dev)
+        sp = ctypes.c_void_p(stream.cuda_stream)
+        d_axes = torch.empty((n, 9), dtype=torch.float32, device=dev)
+        d_imgs = torch.empty((n, N, N), dtype=torch.float32, device=dev)
+        d_sums = torch.empty((2, V, V, V), dtype=torch.float32, device=dev)
+        d_out = torch.empty((N, N, N), dtype=torch.float32, device=dev)
 
     def vp(t):
         return ctypes.c_void_p(t.data_ptr())
@@ -659,16 +807,28 @@ def run_e2e(args, g, vol, axes, world):
     def step():
         check(L.gg_set_volume(h, vp(h_vol), dims), h)
         check(L.gg_forward_project(h, vp(h_axes), n, vp(h_imgs), None), h)
-        check(L.gg_reconstruct_volume(h, vp(h_axes), n, vp(h_imgs), vp(h_out)), h)
+        if world == 1:
+            check(L.gg_reconstruct_volume(h, vp(h_axes), n, vp(h_imgs), vp(h_out)), h)
+            return
+        with torch.cuda.stream(stream):
+            d_axes.copy_(h_axes, non_blocking=True)
+            d_imgs.copy_(h_imgs, non_blocking=True)
+            check(L.gg_back_project_sums_dev(h, vp(d_axes), n, vp(d_imgs), vp(d_sums), sp), h)
+            dist.all_reduce(d_sums)
+            check(L.gg_volume_from_sums_dev(h, vp(d_sums), vp(d_out), sp), h)
+            h_out.copy_(d_out, non_blocking=True)
+        stream.synchronize()
 
     for _ in range(max(1, args.warmup)):
         step()
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step()
     torch.cuda.synchronize()
-    dt = (time.perf_counter() - t0) / args.steps
+    dt = max_over_ranks((time.perf_counter() - t0) / args.steps, device=dev)
     ok = bool(np.isfinite(h_out.numpy()).all())
     h2d = vol.nbytes + 2 * axes.nbytes + n * N * N * 4
     d2h = n * N * N * 4 + vol.nbytes

@@ -143,6 +143,25 @@ int gg_get_volume_dev(gg_gridder *h, float *d_volume_out, void *stream);
 int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int n_axes,
                               const float *d_images, float *d_volume_out, void *stream);
 
+/* Sharded reconstructVol, one gridder per GPU (one process per GPU).  The
+   reference splits the directions over its GPUs (ceil(n/G) each,
+   MultiGPUGridder::PlanCoordinateAxes, MultiGPUGridder.cpp:37-96), each GPU
+   back-projects its slice into its own CAS volume (MultiGPUGridder::BackProject,
+   MultiGPUGridder.cpp:186-269), the volumes are summed on one GPU by peer
+   copies (MultiGPUGridder.cpp:376-411), and reconstructVol divides by the
+   plane density (MultiGPUGridder_Matlab_Class.m:293-311).
+   gg_back_project_sums_dev: this GPU's slice -> d_sums, 2*V^3 floats written
+   (not accumulated): [0, V^3) the CAS volume of the images' back projection,
+   [V^3, 2V^3) the plane density (back projection of all-ones CAS images),
+   both in one fused pass, un-divided.  The caller sums d_sums over the GPUs
+   (one all-reduce or reduce of 2*V^3 floats).
+   gg_volume_from_sums_dev: summed d_sums -> CAS volume sums[0] ./ (sums[1] +
+   1e-6), left resident, then getVol into d_volume_out (N^3).  With one GPU
+   the two calls give gg_reconstruct_volume_dev's result bit for bit. */
+int gg_back_project_sums_dev(gg_gridder *h, const float *d_axes, int n_axes, const float *d_images,
+                             float *d_sums, void *stream);
+int gg_volume_from_sums_dev(gg_gridder *h, const float *d_sums, float *d_volume_out, void *stream);
+
 /* reconstructVol with CTF correction.  The reference carries only the flag
    for it (`ApplyCTFs`, src/Gridders/AbstractGridder.h:118-119) and never
    reads it.  Each image's CAS image is multiplied by its weak-phase CTF

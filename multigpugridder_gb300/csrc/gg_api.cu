@@ -1167,6 +1167,45 @@ extern "C" int gg_reconstruct_volume_dev(gg_gridder *h, const float *d_axes, int
     });
 }
 
+extern "C" int gg_back_project_sums_dev(gg_gridder *h, const float *d_axes, int n_axes, const float *d_images,
+                                        float *d_sums, void *stream)
+{
+    return guarded(h, [&] {
+        check_axes_count(n_axes);
+        if (n_axes > 0 && (!d_axes || !d_images)) fail(GG_ERR_INVALID_ARG, "axes and images are required");
+        if (!d_sums) fail(GG_ERR_INVALID_ARG, "sums buffer is NULL");
+        cudaStream_t s = (cudaStream_t)stream;
+        begin_dev(h, s);
+        const size_t V3 = (size_t)h->V * h->V * h->V, NN = (size_t)h->N * h->N;
+        GG_CK(cudaMemsetAsync(d_sums, 0, 2 * V3 * sizeof(float), s));
+        const int B = h->max_batch;
+        for (int a0 = 0; a0 < n_axes; a0 += B) {
+            const int b = std::min(B, n_axes - a0);
+            ensure_slot(h, 0, B, false);
+            bp_batch(h, d_axes + (size_t)a0 * 9, b, d_images + (size_t)a0 * NN, nullptr, d_sums, false, 0, s,
+                     d_sums + V3);
+        }
+        end_dev(h, s);
+    });
+}
+
+extern "C" int gg_volume_from_sums_dev(gg_gridder *h, const float *d_sums, float *d_volume_out, void *stream)
+{
+    return guarded(h, [&] {
+        if (!d_sums || !d_volume_out) fail(GG_ERR_INVALID_ARG, "sums and output are required");
+        cudaStream_t s = (cudaStream_t)stream;
+        begin_dev(h, s);
+        const size_t V3 = (size_t)h->V * h->V * h->V;
+        h->cas.ensure(V3);
+        GG_CK(cudaMemcpyAsync(h->cas.p, d_sums, V3 * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        // tmpCASVolume ./ (PlaneDensity + 1e-6) (MultiGPUGridder_Matlab_Class.m:308)
+        GG_CK(launch_divide_plane_density(h->cas.p, d_sums + V3, V3, 1e-6f, s));
+        do_get_volume(h, h->cas.p, d_volume_out, s);
+        h->cas_fp_valid = false;
+        end_dev(h, s);
+    });
+}
+
 extern "C" int gg_reconstruct_volume_ctf_dev(gg_gridder *h, const float *d_axes, int n_axes, const float *d_images,
                                              const float *d_defocus, const float *d_defocus_v,
                                              const float *d_astig_angle, float voltage_kv, float cs_mm,

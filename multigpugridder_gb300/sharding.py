@@ -41,28 +41,28 @@ def max_over_ranks(x, device="cpu"):
 
 def reconstruct_sharded(backend, axes, images, group=None):
     """reconstructVol over the ranks of `group`: each rank back-projects its
-    slice of (axes, images) into a CAS volume and a plane density
-    (backend.back_project(axes, images) -> two V^3 tensors), one all-reduce
-    sums both, and backend.finish(cas_sum, pd_sum) divides (+1e-6) and returns
-    the volume.  Every rank returns the same volume."""
-    import torch
+    slice of (axes, images) into one buffer of two stacked V^3 sums, the CAS
+    volume and the plane density (backend.back_project(axes, images) ->
+    tensor (2, V, V, V)); one all-reduce sums the buffer in place; and
+    backend.finish(sums) divides (+1e-6) and returns the volume.  Every rank
+    returns the same volume."""
     import torch.distributed as dist
 
     world = dist.get_world_size(group) if dist.is_initialized() else 1
     rank = dist.get_rank(group) if dist.is_initialized() else 0
     start, count = shard(len(axes), world, rank)
-    cas, pd = backend.back_project(axes[start:start + count], images[start:start + count])
-    both = torch.stack([cas, pd])
+    sums = backend.back_project(axes[start:start + count], images[start:start + count])
     if world > 1:
-        dist.all_reduce(both, op=dist.ReduceOp.SUM, group=group)
-    return backend.finish(both[0], both[1])
+        dist.all_reduce(sums, op=dist.ReduceOp.SUM, group=group)
+    return backend.finish(sums)
 
 
 class GridderBackend:
     """The per-rank work of `reconstruct_sharded` on this rank's GPU, through
-    the library's device-pointer calls: the reference-rule back projection of
-    the images and of all-ones CAS images (the plane density), then, after the
-    sum, the division and getVol."""
+    the library's device-pointer calls: gg_back_project_sums_dev (the images'
+    back projection and the plane density in one fused pass, un-divided) and,
+    after the sum over ranks, gg_volume_from_sums_dev (the division and
+    getVol)."""
 
     def __init__(self, gridder, stream=None):
         import torch
@@ -78,39 +78,33 @@ class GridderBackend:
         s = self.stream or torch.cuda.current_stream(self.dev)
         return ctypes.c_void_p(s.cuda_stream)
 
-    def back_project(self, axes, images):
+    def back_project(self, axes, images, out=None):
+        """This rank's sums (2, V, V, V) on its GPU; axes (n, 9) and images
+        (n, N, N), numpy arrays or tensors (moved to the GPU if needed)."""
         import torch
 
         from . import _lib
         from ._lib import check
 
-        L, h, V, M = _lib.lib(), self.h, self.g.V, self.g.M
-        vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
-        ax = torch.as_tensor(np.ascontiguousarray(axes, np.float32)).to(self.dev)
-        im = torch.as_tensor(np.ascontiguousarray(images, np.float32)).to(self.dev)
-        n = ax.shape[0]
-        cas = torch.zeros((V, V, V), dtype=torch.float32, device=self.dev)
-        pd = torch.zeros_like(cas)
-        if n > 0:
-            sp = self._sp()
-            check(L.gg_back_project_dev(h, vp(ax), n, vp(im), None, 0, sp), h)
-            check(L.gg_get_cas_volume_dev(h, vp(cas), sp), h)
-            ones = torch.ones((n, M, M), dtype=torch.float32, device=self.dev)
-            check(L.gg_back_project_dev(h, vp(ax), n, None, vp(ones), 0, sp), h)
-            check(L.gg_get_cas_volume_dev(h, vp(pd), sp), h)
-        return cas, pd
+        L, h, V = _lib.lib(), self.h, self.g.V
+        ax = torch.as_tensor(np.ascontiguousarray(axes, np.float32) if isinstance(axes, np.ndarray) else axes)
+        im = torch.as_tensor(np.ascontiguousarray(images, np.float32) if isinstance(images, np.ndarray) else images)
+        ax = ax.to(self.dev, torch.float32).contiguous()
+        im = im.to(self.dev, torch.float32).contiguous()
+        sums = out if out is not None else torch.empty((2, V, V, V), dtype=torch.float32, device=self.dev)
+        check(L.gg_back_project_sums_dev(h, ctypes.c_void_p(ax.data_ptr()), ax.shape[0],
+                                         ctypes.c_void_p(im.data_ptr()), ctypes.c_void_p(sums.data_ptr()),
+                                         self._sp()), h)
+        return sums
 
-    def finish(self, cas_sum, pd_sum):
+    def finish(self, sums, out=None):
         import torch
 
         from . import _lib
         from ._lib import check
 
         L, h, N = _lib.lib(), self.h, self.g.VolumeSize
-        vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
-        div = (cas_sum / (pd_sum + 1e-6)).contiguous()  # tmpCASVolume ./ (PlaneDensity + 1e-6)
-        out = torch.empty((N, N, N), dtype=torch.float32, device=self.dev)
-        sp = self._sp()
-        check(L.gg_set_cas_volume_dev(h, vp(div), sp), h)
-        check(L.gg_get_volume_dev(h, vp(out), sp), h)
-        return out
+        vol = out if out is not None else torch.empty((N, N, N), dtype=torch.float32, device=self.dev)
+        check(L.gg_volume_from_sums_dev(h, ctypes.c_void_p(sums.data_ptr()), ctypes.c_void_p(vol.data_ptr()),
+                                        self._sp()), h)
+        return vol

@@ -11,10 +11,13 @@ kernels (gg_oracle.c, OpenMP over all host threads).  FFTs use scipy.fft with
 every worker thread.
 
 One bench step of the GPU path processes D directions (forward projection,
-back projection, plane-density back projection).  On the CPU a bounded sample
-of S of those directions is timed, plus the direction-independent work (CAS
-volume preparation, getVol), and the step time is extrapolated:
-    t_step(D) = t_fixed + (D / S) * t_sample(S).
+back projection, plane-density back projection).  On the CPU one step runs
+the same path on a bounded sample of S of those directions: the
+direction-independent work (CAS volume preparation, getVol) and the
+per-direction work of the S directions.  Its measured duration is
+t_sample_step = t_fixed + t_sample(S); the D-direction step it stands for is
+extrapolated as t_step(D) = t_fixed + (D / S) * t_sample(S) and reported
+apart.
 """
 import os
 import time
@@ -84,7 +87,8 @@ def cas_imgs_from_imgs_f32(x, M, workers):
 
 
 def time_step(vol, axes_sample, p, n_directions, threads=None):
-    """Time one extrapolated step; returns (t_step_seconds, details)."""
+    """Time one step on the sample; returns (measured seconds, details with
+    the extrapolated full-step time t_step_extrapolated_s)."""
     threads = threads or host_threads()
     O.set_threads(threads)
     t0 = time.perf_counter()
@@ -113,8 +117,8 @@ def time_step(vol, axes_sample, p, n_directions, threads=None):
     S = len(axes_sample)
     per_dir = (t_fp + t_ifft + t_fft + t_bp + t_pd) / S
     t_fixed = t_prep + t_get
-    t_step = t_fixed + n_directions * per_dir
+    t_measured = t_fixed + per_dir * S
     details = {"threads": threads, "sample_directions": S, "t_fixed_s": t_fixed, "t_per_direction_s": per_dir,
                "t_fp_s": t_fp, "t_bp_s": t_bp, "t_density_s": t_pd, "t_fft2_s": t_ifft + t_fft,
-               "finite": bool(np.isfinite(rec).all())}
-    return t_step, details
+               "t_step_extrapolated_s": t_fixed + n_directions * per_dir, "finite": bool(np.isfinite(rec).all())}
+    return t_measured, details

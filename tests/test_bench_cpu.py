@@ -26,3 +26,15 @@ def test_reference_arm_json_line():
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and "8 of the 64" in cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["N"] == 32 and d["config"]["directions"] == 64
+    # the line reports what it timed: value = the sample's directions / the measured step time
+    assert d["directions_per_step"] == 8
+    assert abs(d["value"] - 8 / (d["ms_per_step"] / 1e3)) <= 1e-9 * d["value"]
+    assert d["full_step_extrapolated"]["value"] > 0
+    # and the same config dict as the GPU arm
+    import argparse
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    ns = argparse.Namespace(size=32, directions=64, batch=2000, precision="f32")
+    assert d["config"] == bench.bench_config(ns, 1)

@@ -69,3 +69,57 @@ def test_forward_projection_at_256_matches_oracle(cuda):
     assert O.rel_l2(cas, ref_cas) < TOL
     ref = O.imgs_from_cas_imgs(ref_cas.astype(np.float64), N)
     assert O.rel_l2(imgs, ref) < TOL
+
+
+def test_benchmark_workload_matches_oracle(cuda):
+    """The benchmark's own configuration through the device-pointer calls it
+    times: 128^3 (100 blobs, seed 2), interpFactor 2 (CAS images 256^2, CAS
+    volume 262^3), the 100 x 100 azimuth x cos-polar direction grid,
+    MaxAxesToAllocate 2000.  forwardProject of all 10,000 directions (five
+    device batches) is checked on a fixed subset of 500 directions against
+    the oracle's FP32 restatement; reconstructVol of those 500 images is
+    checked against the oracle's FP32 reconstructVol (plane density and
+    a / (b + 1e-6), MultiGPUGridder_Matlab_Class.m:284-312).  Relative L2
+    <= 1e-5."""
+    import ctypes
+
+    import torch
+
+    import multigpugridder_gb300 as gg
+    from multigpugridder_gb300 import synthetic
+    from multigpugridder_gb300._lib import check, lib
+
+    N, n, S = 128, 10000, 500
+    p = O.Params(N)
+    vol = synthetic.blob_volume(N, 100, seed=2)
+    axes = synthetic.grid_axes(100, 100).astype(np.float32)
+    sub = np.linspace(0, n - 1, S).round().astype(int)
+    L = lib()
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    g = gg.MultiGPUGridder(N, n, 2.0, MaxAxesToAllocate=2000)
+    try:
+        h = g.handle
+        s = ctypes.c_void_p(torch.cuda.current_stream(cuda).cuda_stream)
+        d_vol = torch.from_numpy(vol).to(cuda)
+        d_ax = torch.from_numpy(axes).to(cuda)
+        d_img = torch.full((n, N, N), float("nan"), device=cuda)
+        check(L.gg_set_volume_dev(h, vp(d_vol), s), h)
+        check(L.gg_forward_project_dev(h, vp(d_ax), n, vp(d_img), None, s), h)
+        d_sub_ax = d_ax[torch.from_numpy(sub).to(cuda)].contiguous()
+        d_sub_img = d_img[torch.from_numpy(sub).to(cuda)].contiguous()
+        d_rec = torch.full((N, N, N), float("nan"), device=cuda)
+        check(L.gg_reconstruct_volume_dev(h, vp(d_sub_ax), S, vp(d_sub_img), vp(d_rec), s), h)
+        torch.cuda.synchronize()
+        imgs = d_sub_img.cpu().numpy()
+        rec = d_rec.cpu().numpy()
+    finally:
+        g.close()
+    assert np.all(np.isfinite(imgs)) and np.all(np.isfinite(rec))
+    ref_imgs, _ = O.forward_project(vol, axes[sub], p, precision="f32")
+    e_img = O.rel_l2(imgs, ref_imgs)
+    ref_rec, _, _ = O.reconstruct_vol(imgs, axes[sub], p, precision="f32")
+    e_rec = O.rel_l2(rec, ref_rec)
+    print("benchmark workload, %d of %d directions: images rel-L2 %.2e, reconstructVol rel-L2 %.2e"
+          % (S, n, e_img, e_rec))
+    assert e_img < TOL
+    assert e_rec < TOL

@@ -1,7 +1,14 @@
-"""reconstruct_sharded with the library's CUDA backend on one rank (no
-process group): the back projections of the images and of all-ones CAS images,
-the division and getVol give gg_reconstruct_volume's volume within relative L2
-1e-6 (the fused kernel forms the same two sums in one pass)."""
+"""reconstruct_sharded with the library's CUDA backend.
+
+* One rank (no process group): gg_back_project_sums_dev and
+  gg_volume_from_sums_dev give gg_reconstruct_volume_dev's volume bit for bit
+  (the same fused back projection, division and getVol).
+* Two shards on one GPU, run one after the other (no kernel waits on another
+  rank): each shard's CUDA sums, added as the all-reduce would add them,
+  then finished, equal the oracle's reconstructVol over all directions within
+  relative L2 1e-5 (the parity bound; the shards only reorder the float sums
+  of the two halves).
+"""
 import ctypes
 
 import numpy as np
@@ -21,12 +28,58 @@ def test_sharded_reconstruct_single_rank_equals_reconstruct_volume(cuda):
     N = 32
     axes = O.quaternion_axes(60, 91).astype(np.float32)
     imgs = np.random.default_rng(92).standard_normal((60, N, N)).astype(np.float32)
-    g = gg.MultiGPUGridder(N, 60, 2.0, adjustInterpFactor=False)
-    got = reconstruct_sharded(GridderBackend(g), axes, imgs).cpu().numpy()
-    torch.cuda.synchronize()
-    ref = np.empty((N, N, N), np.float32)
-    L = gg.lib()
-    assert L.gg_reconstruct_volume(g.handle, axes.ctypes.data, 60, imgs.ctypes.data, ref.ctypes.data) == 0
-    g.close()
+    g = gg.MultiGPUGridder(N, 60, 2.0, MaxAxesToAllocate=16, adjustInterpFactor=False)
+    try:
+        got = reconstruct_sharded(GridderBackend(g), axes, imgs).cpu().numpy()
+        d_ax, d_img = torch.from_numpy(axes).to(cuda), torch.from_numpy(imgs).to(cuda)
+        d_ref = torch.empty((N, N, N), device=cuda)
+        s = ctypes.c_void_p(torch.cuda.current_stream(cuda).cuda_stream)
+        vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        assert gg.lib().gg_reconstruct_volume_dev(g.handle, vp(d_ax), 60, vp(d_img), vp(d_ref), s) == 0
+        ref = d_ref.cpu().numpy()
+    finally:
+        g.close()
     assert np.all(np.isfinite(got))
-    assert O.rel_l2(got, ref) < 1e-6
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("N,n", [(32, 70), (64, 41)])
+def test_two_shards_through_the_sum_match_oracle(cuda, N, n):
+    import torch
+
+    import multigpugridder_gb300 as gg
+    from multigpugridder_gb300.sharding import GridderBackend, shard
+
+    p = O.Params(N)
+    vol = O.blob_volume(N, 8, seed=93 + N)
+    axes = O.quaternion_axes(n, 94 + N).astype(np.float32)
+    g = gg.MultiGPUGridder(N, n, 2.0, MaxAxesToAllocate=16, adjustInterpFactor=False)
+    try:
+        g.setVolume(vol)
+        imgs = g.forwardProject(axes)
+        be = GridderBackend(g)
+        total = None
+        for r in range(2):
+            s0, c = shard(n, 2, r)
+            part = be.back_project(axes[s0:s0 + c], imgs[s0:s0 + c])
+            total = part.clone() if total is None else total + part
+        got = be.finish(total).cpu().numpy()
+        torch.cuda.synchronize()
+    finally:
+        g.close()
+    ref, _, _ = O.reconstruct_vol(imgs, axes, p, precision="f32")
+    err = O.rel_l2(got, ref)
+    print("two shards N=%d n=%d: rel-L2 %.2e against the oracle's whole-set reconstructVol" % (N, n, err))
+    assert err < 1e-5
+
+
+def test_sums_entry_points_reject_bad_arguments(cuda):
+    import multigpugridder_gb300 as gg
+
+    g = gg.MultiGPUGridder(16, 4, 2.0, adjustInterpFactor=False)
+    try:
+        L = gg.lib()
+        assert L.gg_back_project_sums_dev(g.handle, None, 3, None, None, None) != 0
+        assert L.gg_volume_from_sums_dev(g.handle, None, None, None) != 0
+    finally:
+        g.close()

@@ -1,8 +1,14 @@
 """The N > 1 path on CPU: the reference's direction slicing, the max over
-ranks the benchmark times with, and reconstructVol sharded over two gloo ranks
-(the oracle's reference-rule back projection as each rank's work) equal to one
-process over all directions within relative L2 1e-6 (only the order of the
-float sums differs)."""
+ranks the benchmark times with, and reconstructVol sharded over two gloo ranks.
+
+Each rank's work is a backend with the CUDA backend's interface
+(sharding.GridderBackend): back_project(axes, images N x N) -> one (2, V, V, V)
+tensor of un-divided sums (CAS volume, plane density), finish(sums) -> the
+N^3 volume.  Here that work is the oracle's (images -> CAS images, the
+reference-rule back projections in FP32, the division, getVol), and the
+sharded result must equal the oracle's reconstructVol over all directions
+in one process within relative L2 1e-6 (only the order of the float sums of
+the two ranks' parts differs)."""
 import os
 import socket
 
@@ -36,20 +42,35 @@ def _free_port():
 
 
 class _OracleBackend:
+    """GridderBackend's interface and result shapes, computed by the oracle."""
+
     def __init__(self, p):
         self.p = p
 
-    def back_project(self, axes, cas_images):
+    def back_project(self, axes, images):
         import torch
 
         p = self.p
-        cas = O.bp_ref_f32(cas_images, axes, p.V, p.mask_radius, p.ker) if len(axes) else np.zeros((p.V,) * 3, np.float32)
-        pd = (O.bp_ref_f32(np.ones_like(cas_images), axes, p.V, p.mask_radius, p.ker) if len(axes)
-              else np.zeros((p.V,) * 3, np.float32))
-        return torch.from_numpy(np.ascontiguousarray(cas)), torch.from_numpy(np.ascontiguousarray(pd))
+        sums = np.zeros((2,) + (p.V,) * 3, np.float32)
+        if len(axes):
+            ci = O.cas_imgs_from_imgs(np.asarray(images, np.float64), p.M).astype(np.float32)
+            sums[0] = O.bp_ref_f32(ci, axes, p.V, p.mask_radius, p.ker)
+            sums[1] = O.bp_ref_f32(np.ones_like(ci), axes, p.V, p.mask_radius, p.ker)
+        return torch.from_numpy(sums)
 
-    def finish(self, cas, pd):
-        return cas / (pd + 1e-6)
+    def finish(self, sums):
+        import torch
+
+        cas = (sums[0] / (sums[1] + 1e-6)).numpy().astype(np.float64)
+        return torch.from_numpy(O.vol_from_cas(cas, self.p.N).astype(np.float32))
+
+
+def _case():
+    N = 16
+    p = O.Params(N)
+    axes = O.quaternion_axes(9, 8).astype(np.float32)
+    imgs = O.blob_volume(N, 5, seed=9)[:9] + np.random.default_rng(7).standard_normal((9, N, N)).astype(np.float32)
+    return p, axes, imgs.astype(np.float32)
 
 
 def _worker(rank, world, port, out_dir):
@@ -61,10 +82,7 @@ def _worker(rank, world, port, out_dir):
     dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
     try:
         m = max_over_ranks(1.0 + rank * 2.5)
-        p = O.Params(16)
-        rng = np.random.default_rng(7)
-        axes = O.quaternion_axes(9, 8).astype(np.float32)
-        imgs = rng.standard_normal((9, p.M, p.M)).astype(np.float32)
+        p, axes, imgs = _case()
         vol = reconstruct_sharded(_OracleBackend(p), axes, imgs)
         np.save(os.path.join(out_dir, "vol%d.npy" % rank), vol.numpy())
         np.save(os.path.join(out_dir, "max%d.npy" % rank), np.array([m]))
@@ -78,13 +96,10 @@ def test_reconstruct_sharded_over_two_gloo_ranks(tmp_path):
 
     world = 2
     mp.start_processes(_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
-    p = O.Params(16)
-    rng = np.random.default_rng(7)
-    axes = O.quaternion_axes(9, 8).astype(np.float32)
-    imgs = rng.standard_normal((9, p.M, p.M)).astype(np.float32)
-    whole = _OracleBackend(p).back_project(axes, imgs)
-    ref = (whole[0] / (whole[1] + 1e-6)).numpy()
+    p, axes, imgs = _case()
+    ref, _, _ = O.reconstruct_vol(imgs, axes, p, precision="f32")
     for r in range(world):
         got = np.load(tmp_path / ("vol%d.npy" % r))
+        assert got.shape == (p.N,) * 3
         assert O.rel_l2(got, ref) < 1e-6
         assert float(np.load(tmp_path / ("max%d.npy" % r))[0]) == 3.5
