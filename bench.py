@@ -241,8 +241,8 @@ def run_gb300(args):
     M, V, R = g.M, g.V, int(g.MaskRadius)
     stream = torch.cuda.Stream(device=dev)
     sp = ctypes.c_void_p(stream.cuda_stream)
-    d_vol = torch.from_numpy(vol).to(dev)
-    d_axes = torch.from_numpy(axes).to(dev)
+    d_vol = torch.from_numpy(np.ascontiguousarray(vol)).to(dev)
+    d_axes = torch.from_numpy(np.ascontiguousarray(axes)).to(dev)
     d_imgs = torch.empty((n, N, N), dtype=torch.float32, device=dev)
     d_out = torch.empty((N, N, N), dtype=torch.float32, device=dev)
     d_sums = torch.empty((2, V, V, V), dtype=torch.float32, device=dev) if world > 1 else None
@@ -559,8 +559,8 @@ def run_precision(args):
     L = lib()
     N, n, vol, axes, sub = precision_workload()
     dev = torch.device("cuda", torch.cuda.current_device())
-    d_vol = torch.from_numpy(vol).to(dev)
-    d_axes = torch.from_numpy(axes).to(dev)
+    d_vol = torch.from_numpy(np.ascontiguousarray(vol)).to(dev)
+    d_axes = torch.from_numpy(np.ascontiguousarray(axes)).to(dev)
     d_sub = torch.from_numpy(sub).to(dev)
     d_sub_axes = d_axes[d_sub].contiguous()
     stream = torch.cuda.Stream(device=dev)
@@ -743,8 +743,8 @@ def run_ctf(args, vol, axes):
     s = torch.cuda.current_stream(dev)
     sp = ctypes.c_void_p(s.cuda_stream)
     vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
-    d_vol = torch.from_numpy(vol).to(dev)
-    d_ax = torch.from_numpy(axes).to(dev)
+    d_vol = torch.from_numpy(np.ascontiguousarray(vol)).to(dev)
+    d_ax = torch.from_numpy(np.ascontiguousarray(axes)).to(dev)
     d_img = torch.empty((n, N, N), device=dev)
     d_out = torch.empty((N, N, N), device=dev)
     df = torch.from_numpy(np.random.default_rng(9).uniform(8000.0, 25000.0, n).astype(np.float32)).to(dev)
@@ -788,8 +788,8 @@ def run_e2e(args, g, vol, axes, world, dev):
     L = lib()
     h = g.handle
     n, N, V = len(axes), args.size, g.V
-    h_vol = torch.from_numpy(vol).pin_memory()
-    h_axes = torch.from_numpy(axes).pin_memory()
+    h_vol = torch.from_numpy(np.ascontiguousarray(vol)).pin_memory()
+    h_axes = torch.from_numpy(np.ascontiguousarray(axes)).pin_memory()
     h_imgs = torch.empty((n, N, N), dtype=torch.float32).pin_memory()
     h_out = torch.empty((N, N, N), dtype=torch.float32).pin_memory()
     dims = (ctypes.c_int * 3)(N, N, N)

@@ -25,9 +25,10 @@ def blob_volume(N, n_blobs, seed, dtype=np.float32):
     gx = np.exp(-((x[None, :] - c[:, 0:1]) ** 2) * inv)
     gy = np.exp(-((x[None, :] - c[:, 1:2]) ** 2) * inv)
     gz = np.exp(-((x[None, :] - c[:, 2:3]) ** 2) * inv) * a[:, None]
-    # vol[k, j, i] = sum_b gz[b, k] gy[b, j] gx[b, i]
+    # vol[k, j, i] = sum_b gz[b, k] gy[b, j] gx[b, i]; einsum may return any
+    # memory order, and callers hand the buffer to the C ABI (x fastest)
     vol = np.einsum("bk,bj,bi->kji", gz, gy, gx, optimize=True)
-    return vol.astype(dtype)
+    return np.ascontiguousarray(vol, dtype=dtype)
 
 
 def quaternion_axes(n, seed):

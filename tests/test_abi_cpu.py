@@ -104,6 +104,12 @@ def test_synthetic_inputs_match_the_oracle_generators():
     from oracle import oracle as O
 
     assert np.array_equal(synthetic.blob_volume(24, 10, seed=5), O.blob_volume(24, 10, seed=5))
+    # the buffers go to the C ABI by pointer, so the memory order must be C (x fastest)
+    for N in (24, 128):
+        v = synthetic.blob_volume(N, 10, seed=5)
+        assert v.flags["C_CONTIGUOUS"] and v.dtype == np.float32
+    for a in (synthetic.quaternion_axes(16, 6), synthetic.grid_axes(4, 4)):
+        assert a.flags["C_CONTIGUOUS"]
     assert np.array_equal(synthetic.quaternion_axes(64, 6).astype(np.float32), O.quaternion_axes(64, 6).astype(np.float32))
     assert np.array_equal(synthetic.grid_axes(12, 10).astype(np.float32), O.grid_axes(12, 10).astype(np.float32))
 
