@@ -83,6 +83,14 @@ def workload(args, rank=0, world=1):
 
 FLUSH_BYTES = 512 << 20  # untimed write between steps: 4x the 126 MB L2
 
+# From one-launch ncu captures of the fused back projection at 128^3 x 2,
+# 1,024 directions per launch (profiles/bp_ref_compact_kernel_density_128cubed_1024dirs.md):
+# DRAM bytes (read + write) and L2 bytes per direction, and the fraction of
+# cycles the schedulers issued.
+NCU_BP_DRAM_PER_DIR = 540.3e6 / 1024
+NCU_BP_LTS_PER_DIR = None
+NCU_BP_ISSUE_ACTIVE = 0.715
+
 
 def sizes(args):
     """(N, M, V) of the workload: interpFactor 2, extra padding 3."""
@@ -324,16 +332,24 @@ def run_gb300(args):
             peaks = json.load(f)
     except (OSError, ValueError):
         pass
-    peak = peaks.get("hbm_gbs") or 6800.0
-    # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of
-    # the dominant kernel, the mean over the 10 launches of a one-pass ncu
-    # capture of this workload at full size; null for other shapes
-    traffic = None
-    if dom == "back" and fused and N == 128 and args.batch == 2000 and args.precision == "f32" and n == 10000:
-        traffic = 1.74e9
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": "measured" if peaks.get("hbm_gbs") else "fallback",
-                "traffic": traffic, "bytes_per_unit": bpu[dom], "units_per_launch": units_per_launch,
+    hbm = peaks.get("hbm_gbs") or 6800.0
+    # the L2 read bandwidth of this GPU, measured here (the bound SURVEY-style
+    # accounting names for 128^3: the 72 MB CAS volume stays in the 126 MB L2)
+    l2 = ctypes.c_double()
+    check(L.gg_measure_l2_read_gbs(10, ctypes.byref(l2)))
+    # per-launch DRAM and L2 bytes of the dominant kernel from one-launch ncu
+    # captures of this workload (profiles/), scaled by directions per launch
+    traffic = lts = issue = None
+    if dom == "back" and fused and N == 128 and args.precision == "f32":
+        traffic = NCU_BP_DRAM_PER_DIR * units_per_launch
+        lts = NCU_BP_LTS_PER_DIR * units_per_launch if NCU_BP_LTS_PER_DIR else None
+        issue = NCU_BP_ISSUE_ACTIVE
+    roofline = {"bound": "l2", "kernel": dom, "achieved": achieved, "peak": l2.value, "unit": "GB/s",
+                "frac": achieved / l2.value, "peak_source": "measured in this run (gg_measure_l2_read_gbs, best of 10)",
+                "traffic": traffic, "lts_bytes": lts, "bytes_per_unit": bpu[dom], "units_per_launch": units_per_launch,
+                "hbm": {"peak": hbm, "frac": achieved / hbm,
+                        "peak_source": "measured (MEASURED_PEAKS.json)" if peaks.get("hbm_gbs") else "fallback"},
+                "issue_active": issue,
                 "kernel_ms": {k: v[0] / args.steps for k, v in prof.items()}}
 
     e2e = None

@@ -282,6 +282,12 @@ int gg_precomp(int M, int ker_hwidth, double *precomp_out);
 #define GG_KERNEL_BACK 1      /* back projection kernel (images) */
 #define GG_KERNEL_DENSITY 2   /* back projection of all-ones images (plane density) */
 
+/* L2 read bandwidth of the current device in GB/s, the peak the projection
+   kernels' L2 roofline is taken against: a buffer of about 40% of the L2
+   read repeatedly with L2-only loads by 4 CTAs per SM, best of `runs`
+   event-timed launches.  Allocates and frees its own buffer. */
+int gg_measure_l2_read_gbs(int runs, double *gbs_out);
+
 /* Number of kernels this library has launched in the process so far. */
 long long gg_kernel_launch_count(void);
 /* Per-handle kernel timing with CUDA events recorded around each projection

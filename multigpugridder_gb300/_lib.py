@@ -72,6 +72,7 @@ SIGNATURES = {
     "gg_get_volume_dev": (_c_int, [_vp, _fp, _vp]),
     "gg_reconstruct_volume_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _vp]),
     "gg_back_project_sums_dev": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _vp]),
+    "gg_measure_l2_read_gbs": (_c_int, [_c_int, _dp]),
     "gg_volume_from_sums_dev": (_c_int, [_vp, _fp, _fp, _vp]),
     "gg_reconstruct_volume_ctf": (_c_int, [_vp, _fp, _c_int, _fp, _fp, _fp, _fp, _c_float, _c_float, _c_float,
                                            _c_float, _fp]),

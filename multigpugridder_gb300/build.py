@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgg_gridder.so")
 INCLUDE = os.path.join(ROOT, "include")
-SOURCES = ["gg_project.cu", "gg_cas.cu", "gg_api.cu", "gg_noalloc.cu", "gg_serve.cu", "gg_compat.cu", "gg_fft2.cu", "gg_kb.cpp"]
+SOURCES = ["gg_project.cu", "gg_cas.cu", "gg_api.cu", "gg_noalloc.cu", "gg_serve.cu", "gg_compat.cu", "gg_fft2.cu",
+           "gg_measure.cu", "gg_kb.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -167,6 +167,7 @@ struct gg_gridder {
         DevBuf<float> casimg, real, img;
         DevBuf<cufftComplex> spec;
         DevBuf<uint16_t> casimg_lp;
+        DevBuf<int> order; // the forward projection's direction order (grouped by copy)
         PinBuf stage;
         cudaEvent_t ev_ready = nullptr, ev_free = nullptr;
     } slot[2];
@@ -237,6 +238,7 @@ void ensure_slot(gg_gridder *h, int s, int b, bool need_img)
     sl.spec.ensure(H * b);
     if (need_img) sl.img.ensure(NN * b);
     if (h->img_prec() != kF32) sl.casimg_lp.ensure(MM * b);
+    sl.order.ensure(b);
     if (!sl.ev_ready) GG_CK(cudaEventCreateWithFlags(&sl.ev_ready, cudaEventDisableTiming));
     if (!sl.ev_free) {
         GG_CK(cudaEventCreateWithFlags(&sl.ev_free, cudaEventDisableTiming));
@@ -371,7 +373,8 @@ void fp_batch(gg_gridder *h, const float *d_axes, int b, float *cas_out, float *
     GG_CK(launch_forward_project(dense ? h->cas.p : h->cas_fp.p, h->prec, dense ? h->V : fp_pitch(h->V), cas_out,
                                  h->ker.p, d_axes, b, h->geom(), h->five_taps, h->vol_scale(), s,
                                  dense ? (const void *)h->cas_y.p : (const void *)(h->cas_fp.p + fp_copy_floats(h)),
-                                 dense ? (const void *)h->cas_z.p : (const void *)(h->cas_fp.p + 2 * fp_copy_floats(h))));
+                                 dense ? (const void *)h->cas_z.p : (const void *)(h->cas_fp.p + 2 * fp_copy_floats(h)),
+                                 S.order.p));
     ps.done();
     if (img_out && h->fused_fft) {
         GG_CK(launch_cas_to_images_fused(cas_out, h->M, h->N, b, img_out, s));

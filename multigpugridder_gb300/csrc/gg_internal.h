@@ -37,11 +37,14 @@ struct Geom {
 // pitch, with y and z as the contiguous axis (launch_transpose_volume for
 // dense FP32, launch_pitch_volume layouts 1 and 2 for FP16/BF16); each
 // direction then reads the copy whose contiguous axis is the most
-// perpendicular to it.
+// perpendicular to it.  d_order (optional, n ints of scratch, used with the
+// copies): the directions then run grouped by the copy they read (a stable
+// partition computed on the device), so that one copy at a time is hot in
+// L2; each image is still written at its direction's slot.
 cudaError_t launch_forward_project(const void *d_vol, int vprec, int pitch, float *d_img, const float *d_ker,
                                    const float *d_axes, int n, const Geom &g, bool five_taps,
                                    const float *d_scale, cudaStream_t s, const void *d_vol_y = nullptr,
-                                   const void *d_vol_z = nullptr);
+                                   const void *d_vol_z = nullptr, int *d_order = nullptr);
 // FP32 volume V^3 (x fastest) -> the same volume with y (layout 1: [z][x][y])
 // or z (layout 2: [y][x][z]) as the contiguous axis.
 cudaError_t launch_transpose_volume(const float *d_in, int V, float *d_out, int layout, cudaStream_t s);

@@ -149,6 +149,70 @@ __device__ __forceinline__ void ld8(const __nv_bfloat16 *p, float v[8])
     }
 }
 
+// The copy a TR forward projection reads for a direction (layout 0: x,
+// 1: y, 2: z contiguous): the one whose contiguous axis is the most
+// perpendicular to the viewing direction (ax + 6 .. ax + 8).
+__device__ __forceinline__ int fp_copy_of(const float *ax)
+{
+    const float nz0 = fabsf(__ldg(ax + 6)), nz1 = fabsf(__ldg(ax + 7)), nz2 = fabsf(__ldg(ax + 8));
+    return (nz1 < nz0 && nz1 <= nz2) ? 1 : (nz2 < nz0 && nz2 < nz1) ? 2 : 0;
+}
+
+// Directions of a TR launch grouped by the copy they read: order[] lists the
+// directions reading copy 0, then copy 1, then copy 2, each group in
+// direction order (a stable partition).  The forward projection runs its
+// work in this order, so that at any time the directions in flight read one
+// copy of the volume (72 MB at 128^3) instead of all three (216 MB, more
+// than the 126 MB L2).  One CTA: counts, then each chunk of 1,024
+// directions scattered with warp ballots and the running offsets.
+constexpr int kOrdThreads = 1024;
+
+__global__ void __launch_bounds__(kOrdThreads) fp_order_kernel(const float *__restrict__ axes, int n, int *__restrict__ order)
+{
+    __shared__ int cnt[3], base[3];
+    __shared__ int wcnt[kOrdThreads / 32][3];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < 3) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    int c[3] = {0, 0, 0};
+    for (int a = threadIdx.x; a < n; a += kOrdThreads) c[fp_copy_of(axes + 9 * (size_t)a)]++;
+#pragma unroll
+    for (int l = 0; l < 3; l++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c[l] += __shfl_xor_sync(0xffffffffu, c[l], o);
+        if (lane == 0) atomicAdd(&cnt[l], c[l]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        base[0] = 0;
+        base[1] = cnt[0];
+        base[2] = cnt[0] + cnt[1];
+    }
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+    for (int c0 = 0; c0 < n; c0 += kOrdThreads) {
+        const int a = c0 + threadIdx.x;
+        const int l = a < n ? fp_copy_of(axes + 9 * (size_t)a) : 3;
+        unsigned m[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) m[k] = __ballot_sync(0xffffffffu, l == k);
+        if (lane < 3) wcnt[warp][lane] = __popc(m[lane]);
+        __syncthreads();
+        if (l < 3) {
+            int pos = base[l] + __popc(m[l] & lt);
+            for (int w = 0; w < warp; w++) pos += wcnt[w][l];
+            order[pos] = a;
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            int t = 0;
+            for (int w = 0; w < kOrdThreads / 32; w++) t += wcnt[w][threadIdx.x];
+            base[threadIdx.x] += t;
+        }
+        __syncthreads();
+    }
+}
+
 // TR: two more copies of the volume with y and z as the contiguous axis
 // (volY[z][x][y], volZ[y][x][z]).  A warp's 8x4 pixels touch about
 // 32 |n . e_c| + (perimeter) distinct volume rows per gather, e_c the
@@ -162,7 +226,7 @@ __global__ void __launch_bounds__(kFpThreads)
 fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int M,
           const float *__restrict__ axes, int maskR, const float *__restrict__ ker, int kerSize,
           float kerHW, int tilesX, long long nItems, const float *__restrict__ d_scale,
-          const TV *__restrict__ volY, const TV *__restrict__ volZ)
+          const TV *__restrict__ volY, const TV *__restrict__ volZ, const int *__restrict__ order)
 {
     const float outScale = d_scale ? *d_scale : 1.0f;
     __shared__ float sker[kMaxKerSize];
@@ -185,16 +249,16 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
 
     const bool items32 = nItems <= 0x7fffffffLL; // 32-bit division per item whenever it fits
     for (long long item = blockIdx.x; item < nItems; item += gridDim.x) {
-        const int a = items32 ? (int)((unsigned)item / (unsigned)tilesPerImg) : (int)(item / tilesPerImg);
-        const int t = (int)(item - (long long)a * tilesPerImg);
+        const int slot = items32 ? (int)((unsigned)item / (unsigned)tilesPerImg) : (int)(item / tilesPerImg);
+        const int t = (int)(item - (long long)slot * tilesPerImg);
+        const int a = order ? __ldg(order + slot) : slot; // the direction (and image) of this work slot
         const float *ax = axes + 9 * (size_t)a;
         // the copy (layout 0: x, 1: y, 2: z contiguous) whose contiguous axis
         // is the most perpendicular to the direction
         int lay = 0;
         bool tall = false;
         if (TR) {
-            const float nz0 = fabsf(__ldg(ax + 6)), nz1 = fabsf(__ldg(ax + 7)), nz2 = fabsf(__ldg(ax + 8));
-            lay = (nz1 < nz0 && nz1 <= nz2) ? 1 : (nz2 < nz0 && nz2 < nz1) ? 2 : 0;
+            lay = fp_copy_of(ax);
             tall = fabsf(__ldg(ax + 3 + lay)) > fabsf(__ldg(ax + lay));
         }
         const int lx = tall ? (lane >> 3) | ((warp & 3) << 2) : (lane & 7) | ((warp & 1) << 3);
@@ -321,11 +385,16 @@ fp_kernel(const TV *__restrict__ vol, int V, int P, float *__restrict__ img, int
 template <typename TV, int TAPS, bool VEC, bool TR = false>
 static cudaError_t launch_fp_t(const TV *vol, int P, float *img, const float *ker, const float *axes, int n,
                                const Geom &g, const float *scale, cudaStream_t s, const TV *volY = nullptr,
-                               const TV *volZ = nullptr)
+                               const TV *volZ = nullptr, int *order = nullptr)
 {
     const int tilesX = (g.M + kFpTile - 1) / kFpTile;
     const long long nItems = (long long)n * tilesX * tilesX;
     if (nItems == 0) return cudaSuccess;
+    if (!TR) order = nullptr;
+    if (order) {
+        fp_order_kernel<<<1, kOrdThreads, 0, s>>>(axes, n, order);
+        count_launches(1);
+    }
     int perSm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, fp_kernel<TV, TAPS, VEC, TR>, kFpThreads, 0);
     if (perSm <= 0) perSm = 1;
@@ -333,7 +402,7 @@ static cudaError_t launch_fp_t(const TV *vol, int P, float *img, const float *ke
     if (grid > nItems) grid = nItems;
     fp_kernel<TV, TAPS, VEC, TR><<<(unsigned)grid, kFpThreads, 0, s>>>(vol, g.V, P, img, g.M, axes, g.mask_radius,
                                                                         ker, g.ker_size, g.ker_hw, tilesX, nItems,
-                                                                        scale, volY, volZ);
+                                                                        scale, volY, volZ, order);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -341,31 +410,35 @@ static cudaError_t launch_fp_t(const TV *vol, int P, float *img, const float *ke
 template <typename TV>
 static cudaError_t launch_fp_p(const void *d_vol, int P, float *d_img, const float *d_ker, const float *d_axes, int n,
                                const Geom &g, bool five_taps, const float *scale, cudaStream_t s,
-                               const void *d_vol_y, const void *d_vol_z)
+                               const void *d_vol_y, const void *d_vol_z, int *d_order)
 {
     const TV *v = (const TV *)d_vol;
     if (five_taps) return launch_fp_t<TV, 5, false>(v, P, d_img, d_ker, d_axes, n, g, scale, s);
     const TV *vy = (const TV *)d_vol_y, *vz = (const TV *)d_vol_z;
     if (sizeof(TV) == 4 && vy && vz && P == g.V)
-        return launch_fp_t<TV, 4, false, true>(v, P, d_img, d_ker, d_axes, n, g, scale, s, vy, vz);
+        return launch_fp_t<TV, 4, false, true>(v, P, d_img, d_ker, d_axes, n, g, scale, s, vy, vz, d_order);
     // 2-byte storage only: with FP32 the 8-element rows double the bytes each
     // tap row moves through L1, which costs more than the loads it saves
     const bool vec = sizeof(TV) == 2 && P % 8 == 0 && P >= g.V + 4 && ((size_t)d_vol & 15) == 0;
     const bool aligned = ((size_t)vy & 15) == 0 && ((size_t)vz & 15) == 0;
-    if (vec && vy && vz && aligned) return launch_fp_t<TV, 4, true, true>(v, P, d_img, d_ker, d_axes, n, g, scale, s, vy, vz);
+    if (vec && vy && vz && aligned)
+        return launch_fp_t<TV, 4, true, true>(v, P, d_img, d_ker, d_axes, n, g, scale, s, vy, vz, d_order);
     if (vec) return launch_fp_t<TV, 4, true>(v, P, d_img, d_ker, d_axes, n, g, scale, s);
     return launch_fp_t<TV, 4, false>(v, P, d_img, d_ker, d_axes, n, g, scale, s);
 }
 
 cudaError_t launch_forward_project(const void *d_vol, int vprec, int pitch, float *d_img, const float *d_ker,
                                    const float *d_axes, int n, const Geom &g, bool five_taps, const float *scale,
-                                   cudaStream_t s, const void *d_vol_y, const void *d_vol_z)
+                                   cudaStream_t s, const void *d_vol_y, const void *d_vol_z, int *d_order)
 {
     if (vprec == kF32)
-        return launch_fp_p<float>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s, d_vol_y, d_vol_z);
+        return launch_fp_p<float>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s, d_vol_y, d_vol_z,
+                                  d_order);
     if (vprec == kF16)
-        return launch_fp_p<__half>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s, d_vol_y, d_vol_z);
-    return launch_fp_p<__nv_bfloat16>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s, d_vol_y, d_vol_z);
+        return launch_fp_p<__half>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s, d_vol_y, d_vol_z,
+                                   d_order);
+    return launch_fp_p<__nv_bfloat16>(d_vol, pitch, d_img, d_ker, d_axes, n, g, five_taps, scale, s, d_vol_y, d_vol_z,
+                                      d_order);
 }
 
 // ---------------------------------------------------------------------------

@@ -156,7 +156,8 @@ void plan_request(Request &r)
     r.chunk = std::min(chunk_for(v.M), pow2ceil(std::max(r.n, 1)));
     const size_t b = (size_t)r.chunk;
     size_t bytes = (size_t)std::max(r.n, 1) * 9 * sizeof(float);
-    bytes += b * (MM * sizeof(float) + H * sizeof(cufftComplex) + MM * sizeof(float) + NN * sizeof(float));
+    bytes += b * (MM * sizeof(float) + H * sizeof(cufftComplex) + MM * sizeof(float) + NN * sizeof(float) +
+                  sizeof(int));
     if (r.op == GG_OP_BACK) bytes += (size_t)v.V * v.V * v.V * sizeof(float);
     r.footprint = bytes;
 }
@@ -237,6 +238,7 @@ void enqueue(gg_server *S, Request &r)
     cufftComplex *d_spec = pool_alloc<cufftComplex>(S, H * B, s);
     float *d_real = pool_alloc<float>(S, MM * B, s);
     float *d_img = pool_alloc<float>(S, NN * B, s);
+    int *d_order = r.op == GG_OP_FORWARD ? pool_alloc<int>(S, B, s) : nullptr;
     float *d_acc = nullptr;
     const size_t V3 = (size_t)v.V * v.V * v.V;
     if (r.n > 0) GS_CK(cudaMemcpyAsync(d_axes, r.axes, (size_t)r.n * 9 * sizeof(float), cudaMemcpyHostToDevice, s));
@@ -250,7 +252,7 @@ void enqueue(gg_server *S, Request &r)
             v.fused_fft ? 0 : lane_plan(L, r.op == GG_OP_FORWARD ? CUFFT_C2R : CUFFT_R2C, v.M, pow2ceil(b));
         if (r.op == GG_OP_FORWARD) {
             GS_CK(launch_forward_project(v.cas, kF32, v.V, d_cas, v.ker, d_axes + (size_t)c0 * 9, b, v.g, v.five_taps,
-                                         nullptr, s, v.cas_y, v.cas_z));
+                                         nullptr, s, v.cas_y, v.cas_z, d_order));
             if (v.fused_fft) {
                 GS_CK(launch_cas_to_images_fused(d_cas, v.M, v.N, b, d_img, s));
             } else {
@@ -278,6 +280,7 @@ void enqueue(gg_server *S, Request &r)
         GS_CK(cudaMemcpyAsync(r.out, d_acc, V3 * sizeof(float), cudaMemcpyDeviceToHost, s));
         GS_CK(cudaFreeAsync(d_acc, s));
     }
+    if (d_order) GS_CK(cudaFreeAsync(d_order, s));
     GS_CK(cudaFreeAsync(d_img, s));
     GS_CK(cudaFreeAsync(d_real, s));
     GS_CK(cudaFreeAsync(d_spec, s));

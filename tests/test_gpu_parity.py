@@ -496,3 +496,13 @@ def test_back_matches_reference_kernel(cuda, gglib, N):
     ref, got = ref.cpu().numpy(), got.cpu().numpy()
     assert O.rel_l2(got, ref) < TOL
     assert O.rel_l2(O.bp_ref_f32(img, axes, p.V, p.mask_radius, p.ker), ref) < TOL
+
+
+def test_l2_read_probe(cuda, gglib):
+    """gg_measure_l2_read_gbs: the L2 read bandwidth the roofline is taken
+    against; a GB300 reads its L2 well above its HBM rate and below 100 TB/s."""
+    gbs = ctypes.c_double()
+    assert gglib.gg_measure_l2_read_gbs(3, ctypes.byref(gbs)) == 0
+    print("L2 read %.0f GB/s" % gbs.value)
+    assert 2000.0 < gbs.value < 100000.0
+    assert gglib.gg_measure_l2_read_gbs(0, ctypes.byref(gbs)) != 0
