@@ -469,15 +469,23 @@ def run_serve(args):
                 if dt > 2e-3:
                     time.sleep(dt - 1e-3)
             hs.append(submit(si, op, n, seed))
-        for h in hs:
-            srv.wait(h)
+        lats = [srv.wait(h)[1] for h in hs]
         el = time.perf_counter() - t0
         st = srv.stats()
         dirs = sum(x[3] for x in sched)
+        # latency percentiles per request class: small (n < 256) and large (n >= 1024)
+        # requests on 64^3/128^3 and on 192^3/256^3 volumes
+        classes = {}
+        for (t, si, op, n, seed), lat in zip(sched, lats):
+            key = "%s_%s" % ("vol64_128" if si < 2 else "vol192_256",
+                             "n_lt_256" if n < 256 else ("n_ge_1024" if n >= 1024 else "n_256_1023"))
+            classes.setdefault(key, []).append(lat)
+        by_class = {k: {"requests": len(v), "p50_ms": float(np.percentile(v, 50)),
+                        "p99_ms": float(np.percentile(v, 99))} for k, v in sorted(classes.items())}
         return {"offered_rps": len(sched) / (sched[-1][0] * scale) if sched else 0.0, "requests": len(sched),
                 "seconds": el, "throughput_rps": len(sched) / el, "directions_per_s": dirs / el,
                 "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
-                "peak_inflight": st["peak_inflight"], "peak_gb": st["peak_gb"]}
+                "peak_inflight": st["peak_inflight"], "peak_gb": st["peak_gb"], "by_class": by_class}
 
     # warm the lanes, then the closed loop: all requests queued at once
     for h in [submit(si, op, min(n, 64), seed) for _, si, op, n, seed in closed[:16]]:

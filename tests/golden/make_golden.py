@@ -2,6 +2,14 @@
 
   python tests/golden/make_golden.py tables      # kb_precomp.npz (CPU)
   python tests/golden/make_golden.py reference   # reference_kernels.npz (GPU)
+  python tests/golden/make_golden.py filters     # reference_filters.npz (GPU)
+
+reference_filters.npz holds small seeded inputs and the outputs of the
+reference's own filter kernels (src/Filters/*Filter.cu, compiled unmodified
+into oracle/_ref/ and launched with their UpdateFilter geometry by
+oracle/ref_kernels.py: RefFilters), and of its two image-stage chains
+(gpuGridder::CASImgsToImgs / ::ImgsToCASImgs, gpuGridder.cpp:432-596:
+those filters and one cuFFT C2C per image).  It must be generated on a GPU.
 
 kb_precomp.npz holds the FP32 KB lookup table the reference hands to its
 kernels (single(getKernelFiltTable(2, 501)), MultiGPUGridder_Matlab_Class.m:128)
@@ -85,6 +93,94 @@ def make_reference(out_path):
     return out_path
 
 
+def make_filters(out_path):
+    import torch
+
+    from oracle.ref_kernels import RefFilters
+
+    dev = torch.device("cuda:0")
+    torch.cuda.init()
+    rf = RefFilters()
+    rng = np.random.default_rng(77)
+    out = {}
+
+    def t(a):
+        return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
+
+    def put(name, x):
+        torch.cuda.synchronize()
+        out[name] = x.cpu().numpy() if hasattr(x, "cpu") else x
+
+    S, NS = 8, 3
+    c2 = rng.standard_normal((NS, S, S, 2)).astype(np.float32)
+    r2 = rng.standard_normal((NS, S, S)).astype(np.float32)
+    r3 = rng.standard_normal((S, S, S)).astype(np.float32)
+    out.update(c2=c2, r2=r2, r3=r3)
+    y = torch.zeros((NS, S, S), device=dev)
+    rf.complex_to_cas(t(c2).data_ptr(), y.data_ptr(), S, NS)
+    put("complex_to_cas_2d", y)
+    y = torch.zeros((NS, S, S, 2), device=dev)
+    rf.cas_to_complex(t(r2).data_ptr(), y.data_ptr(), S, NS)
+    put("cas_to_complex_2d", y)
+    y = torch.zeros((S, S, S, 2), device=dev)
+    rf.cas_to_complex(t(r3).data_ptr(), y.data_ptr(), S, 0)
+    put("cas_to_complex_3d", y)
+    for nm, a, cplx in (("fftshift_2d_real", r2, False), ("fftshift_2d_complex", c2, True)):
+        x = t(a)
+        rf.fftshift_2d(x.data_ptr(), S, NS, cplx)
+        put(nm, x)
+    x = t(r3)
+    rf.fftshift_3d(x.data_ptr(), S, False)
+    put("fftshift_3d_real", x)
+    pin = rng.standard_normal((2, 5, 6)).astype(np.float32)
+    out["pad_in"] = pin
+    y = torch.zeros((2 + 2, 5 + 4, 6 + 2), device=dev)
+    rf.pad_volume(t(pin).data_ptr(), y.data_ptr(), 6, 5, 2, 1, 2, 1)
+    put("pad_out", y)
+    cin = rng.standard_normal((6, 9, 10)).astype(np.float32)
+    out["crop_in"] = cin
+    y = torch.zeros((6 - 2, 9 - 4, 10 - 2), device=dev)
+    rf.crop_volume(t(cin).data_ptr(), y.data_ptr(), 10, 9, 6, 1, 2, 1)
+    put("crop_out", y)
+    a = rng.standard_normal((NS, S, S)).astype(np.float32)
+    b = rng.standard_normal((NS, S, S)).astype(np.float32)
+    a[rng.random(a.shape) < 0.2] = 0.0
+    b[rng.random(b.shape) < 0.2] = 0.0
+    out.update(arith_a=a, arith_b=b)
+    for nm, fn in (("divide", lambda x: rf.divide_volumes(x.data_ptr(), t(b).data_ptr(), S, NS)),
+                   ("multiply", lambda x: rf.multiply_volumes(x.data_ptr(), t(b).data_ptr(), S, NS, False)),
+                   ("add", lambda x: rf.add_volumes(x.data_ptr(), t(b).data_ptr(), S, NS)),
+                   ("divide_scalar", lambda x: rf.divide_scalar(x.data_ptr(), 3.0, S, NS))):
+        x = t(a)
+        fn(x)
+        put(nm, x)
+    x = t(c2)
+    rf.multiply_volumes(x.data_ptr(), t(b).data_ptr(), S, NS, True)
+    put("multiply_complex", x)
+    y = torch.zeros((NS, S, S, 2), device=dev)
+    rf.real_to_complex(t(r2).data_ptr(), y.data_ptr(), S, NS)
+    put("real_to_complex", y)
+    y = torch.zeros((NS, S, S), device=dev)
+    rf.complex_to_real(t(c2).data_ptr(), y.data_ptr(), S, NS)
+    put("complex_to_real", y)
+    # the image stages: CAS images of edge M = 32 <-> images of edge N = 16
+    M, N, n = 32, 16, 3
+    cas = rng.standard_normal((n, M, M)).astype(np.float32)
+    imgs = rng.standard_normal((n, N, N)).astype(np.float32)
+    out.update(chain_cas_in=cas, chain_imgs_in=imgs)
+    w = t(cas)
+    y = torch.zeros((n, N, N), device=dev)
+    cx = torch.zeros((n, M, M, 2), device=dev)
+    rf.cas_imgs_to_imgs(w.data_ptr(), y.data_ptr(), cx.data_ptr(), M, N, n, 2.0)
+    put("chain_imgs_out", y)
+    y = torch.zeros((n, M, M), device=dev)
+    cx = torch.zeros((n, M, M, 2), device=dev)
+    rf.imgs_to_cas_imgs(t(imgs).data_ptr(), y.data_ptr(), cx.data_ptr(), M, N, n)
+    put("chain_cas_out", y)
+    np.savez_compressed(out_path, **out)
+    return out_path
+
+
 if __name__ == "__main__":
     what = sys.argv[1] if len(sys.argv) > 1 else "tables"
     if what == "tables":
@@ -92,5 +188,8 @@ if __name__ == "__main__":
     elif what == "reference":
         dst = sys.argv[2] if len(sys.argv) > 2 else os.path.join(HERE, "reference_kernels.npz")
         print(make_reference(dst))
+    elif what == "filters":
+        dst = sys.argv[2] if len(sys.argv) > 2 else os.path.join(HERE, "reference_filters.npz")
+        print(make_filters(dst))
     else:
-        raise SystemExit("usage: make_golden.py tables|reference [out.npz]")
+        raise SystemExit("usage: make_golden.py tables|reference|filters [out.npz]")

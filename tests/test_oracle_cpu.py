@@ -358,3 +358,47 @@ def test_oracle_matches_reference_kernel_outputs():
         assert np.array_equal(bp, g[key + "_bp"]), key
         # the FP64 oracle is the same operator
         assert O.rel_l2(O.fp_f64(cas, axes, M, R, ker), ref_fp) < 1e-5, key
+
+
+REF_FILTERS = os.path.join(GOLDEN, "reference_filters.npz")
+
+
+@pytest.mark.skipif(not os.path.exists(REF_FILTERS), reason="reference-filter fixtures not generated")
+def test_oracle_matches_reference_filter_outputs():
+    """The oracle's NumPy forms of the filters and image stages against the
+    reference's own filter kernels and cuFFT chain (tests/golden/make_golden.py
+    filters): data movement bit for bit, the CAS -> complex halves within FP32
+    rounding of (a + b) / 2, the two image-stage chains (FP32 cuFFT against the
+    FP64 restatement) within relative L2 1e-5."""
+    g = np.load(REF_FILTERS)
+    c2 = g["c2"][..., 0] + 1j * g["c2"][..., 1]
+    r2, r3 = g["r2"], g["r3"]
+
+    def cplx(x):
+        return x[..., 0] + 1j * x[..., 1]
+
+    # ComplexToCASFilter.cu:3-26 / ToCAS.m:5
+    assert np.array_equal(O.to_cas(c2.astype(np.complex64)), g["complex_to_cas_2d"])
+    # CASToComplexFilter.cu:3-81 / FromCAS.m:7-13, 2-D slices and the 3-D volume
+    assert np.allclose(O.from_cas(r2, axes=(1, 2)), cplx(g["cas_to_complex_2d"]), rtol=1e-6, atol=1e-6)
+    assert np.allclose(O.from_cas(r3), cplx(g["cas_to_complex_3d"]), rtol=1e-6, atol=1e-6)
+    # FFTShift2DFilter.cu / FFTShift3DFilter.cu: fftshift over the slice axes
+    assert np.array_equal(np.fft.fftshift(r2, axes=(1, 2)), g["fftshift_2d_real"])
+    assert np.array_equal(np.fft.fftshift(g["c2"], axes=(1, 2)), g["fftshift_2d_complex"])
+    assert np.array_equal(np.fft.fftshift(r3), g["fftshift_3d_real"])
+    # PadVolumeFilter.cu (into a zeroed output) / CropVolumeFilter.cu
+    assert np.array_equal(np.pad(g["pad_in"], ((1, 1), (2, 2), (1, 1))), g["pad_out"])
+    assert np.array_equal(g["crop_in"][1:-1, 2:-2, 1:-1], g["crop_out"])
+    a, b = g["arith_a"], g["arith_b"]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        # DivideVolumeFilter.cu:24-31: the zero guard
+        assert np.array_equal(np.where((a != 0) & (b != 0), a / b, np.float32(0)), g["divide"])
+    assert np.array_equal(a * b, g["multiply"])
+    assert np.array_equal(g["c2"] * b[..., None], g["multiply_complex"])
+    assert np.array_equal(a + b, g["add"])
+    assert np.array_equal(a / np.float32(3.0), g["divide_scalar"])
+    assert np.array_equal(np.stack([r2, np.zeros_like(r2)], -1), g["real_to_complex"])
+    assert np.array_equal(g["c2"][..., 0], g["complex_to_real"])
+    # the image stages (gpuGridder.cpp:432-518 and :520-596)
+    assert O.rel_l2(O.imgs_from_cas_imgs(g["chain_cas_in"], 16), g["chain_imgs_out"]) < 1e-5
+    assert O.rel_l2(O.cas_imgs_from_imgs(g["chain_imgs_in"], 32), g["chain_cas_out"]) < 1e-5
