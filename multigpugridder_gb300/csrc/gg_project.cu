@@ -633,11 +633,15 @@ __device__ __forceinline__ float fma_sat(float a, float b, float c)
 
 // One voxel's WI x WJ window from the footprint (fbase = its top-left pixel,
 // rows FS apart); table entry floor(P y) is read at
-// tab + bits(y + q.mg) * q.stride.  Sums row by row, as the reference.
-template <bool DENS, int WI, int WJ, int FS, bool DW = false>
+// tab + bits(y + q.mg) * stride.  Sums row by row, as the reference.  TS: the
+// stride in bytes when known at compile time (128 for 32 interleaved table
+// copies, 4 for one), so the address is a shift-add on the integer pipe
+// rather than a multiply on the FMA pipe; 0: q.stride.
+template <bool DENS, int WI, int WJ, int FS, bool DW = false, int TS = 0>
 __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase, unsigned tab, float pi0, float pj0,
                                             float &cumSum, float &cumW, const float *fbase2 = nullptr)
 {
+    const unsigned st = TS ? (unsigned)TS : q.stride;
 #pragma unroll
     for (int jo = 0; jo < WJ; jo++) {
         const float pj = pj0 + (float)jo;
@@ -651,9 +655,9 @@ __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase
             const unsigned b0 = __float_as_uint(__fadd_rd(fma_sat(q0, q.s, q.c0), q.mg));
             const unsigned b1 = __float_as_uint(__fadd_rd(fma_sat(q1, q.s, q.c1), q.mg));
             const unsigned b2 = __float_as_uint(__fadd_rd(fma_sat(q2, q.s, q.c2), q.mg));
-            float w = lds_f32(tab + b0 * q.stride);
-            w = __fmul_rn(w, lds_f32(tab + b1 * q.stride));
-            w = __fmul_rn(w, lds_f32(tab + b2 * q.stride));
+            float w = lds_f32(tab + b0 * st);
+            w = __fmul_rn(w, lds_f32(tab + b1 * st));
+            w = __fmul_rn(w, lds_f32(tab + b2 * st));
             cumSum = __fmaf_rn(fbase[jo * FS + io], w, cumSum);
             if (DENS) cumW = __fadd_rn(cumW, w);
             if (DW) cumW = __fmaf_rn(fbase2[jo * FS + io], w, cumW);
@@ -669,10 +673,11 @@ __device__ __forceinline__ void foot_window(const FootWin &q, const float *fbase
 // time in the same order), is bit-identical to foot_window's.
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 
-template <bool DENS, int WI, int WJ, int FS, bool DW = false>
+template <bool DENS, int WI, int WJ, int FS, bool DW = false, int TS = 0>
 __device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fbase, unsigned tab, float pi0,
                                                float pj0, float &cumSum, float &cumW, const float *fbase2 = nullptr)
 {
+    const unsigned st = TS ? (unsigned)TS : q.stride;
     const float2 nx0 = f2(q.nx0, q.nx0), nx1 = f2(q.nx1, q.nx1), nx2 = f2(q.nx2, q.nx2);
     const float2 vc = f2(q.vc, q.vc), mg = f2(q.mg, q.mg);
 #pragma unroll
@@ -689,12 +694,12 @@ __device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fb
             const float2 b0 = __fadd2_rd(f2(fma_sat(q0.x, q.s, q.c0), fma_sat(q0.y, q.s, q.c0)), mg);
             const float2 b1 = __fadd2_rd(f2(fma_sat(q1.x, q.s, q.c1), fma_sat(q1.y, q.s, q.c1)), mg);
             const float2 b2 = __fadd2_rd(f2(fma_sat(q2.x, q.s, q.c2), fma_sat(q2.y, q.s, q.c2)), mg);
-            const float2 t0 = f2(lds_f32(tab + __float_as_uint(b0.x) * q.stride),
-                                 lds_f32(tab + __float_as_uint(b0.y) * q.stride));
-            const float2 t1 = f2(lds_f32(tab + __float_as_uint(b1.x) * q.stride),
-                                 lds_f32(tab + __float_as_uint(b1.y) * q.stride));
-            const float2 t2 = f2(lds_f32(tab + __float_as_uint(b2.x) * q.stride),
-                                 lds_f32(tab + __float_as_uint(b2.y) * q.stride));
+            const float2 t0 = f2(lds_f32(tab + __float_as_uint(b0.x) * st),
+                                 lds_f32(tab + __float_as_uint(b0.y) * st));
+            const float2 t1 = f2(lds_f32(tab + __float_as_uint(b1.x) * st),
+                                 lds_f32(tab + __float_as_uint(b1.y) * st));
+            const float2 t2 = f2(lds_f32(tab + __float_as_uint(b2.x) * st),
+                                 lds_f32(tab + __float_as_uint(b2.y) * st));
             const float2 w = __fmul2_rn(__fmul2_rn(t0, t1), t2);
             cumSum = __fmaf_rn(fbase[jo * FS + io], w.x, cumSum);
             if (DENS) cumW = __fadd_rn(cumW, w.x);
@@ -712,9 +717,9 @@ __device__ __forceinline__ void foot_window_x2(const FootWin &q, const float *fb
             const unsigned b0 = __float_as_uint(__fadd_rd(fma_sat(q0, q.s, q.c0), q.mg));
             const unsigned b1 = __float_as_uint(__fadd_rd(fma_sat(q1, q.s, q.c1), q.mg));
             const unsigned b2 = __float_as_uint(__fadd_rd(fma_sat(q2, q.s, q.c2), q.mg));
-            float w = lds_f32(tab + b0 * q.stride);
-            w = __fmul_rn(w, lds_f32(tab + b1 * q.stride));
-            w = __fmul_rn(w, lds_f32(tab + b2 * q.stride));
+            float w = lds_f32(tab + b0 * st);
+            w = __fmul_rn(w, lds_f32(tab + b1 * st));
+            w = __fmul_rn(w, lds_f32(tab + b2 * st));
             cumSum = __fmaf_rn(fbase[jo * FS + io], w, cumSum);
             if (DENS) cumW = __fadd_rn(cumW, w);
             if (DW) cumW = __fmaf_rn(fbase2[jo * FS + io], w, cumW);
@@ -821,19 +826,19 @@ template <bool DENS, bool ADJ, bool DW, bool DEEP>
 struct BpGroupMem {
     using Shape = BpShape<ADJ, DW, DEEP>;
     using Q = BpQueue<ADJ, DW, DEEP>;
-    static constexpr int NW = kCThreads / 32, WV = Shape::WV, FP = Shape::FW * (Shape::FW + 1);
+    static constexpr int NW = kCThreads / 32, WV = Shape::WV, FP = Shape::FW * (Shape::FW + (Q::NB == 2 ? 4 : 1));
     BpDirMeta smeta[NW * Q::NB];
     float sax[kBpChunk * 9];
-    int slist[kBpChunk];
+    unsigned short slist[kBpChunk];
     int swarp[kBpChunk / 32]; // kept directions per (pass, warp)
     int scount;
     // per-voxel sums [warp][block voxel]; a voxel is updated by at most one
     // lane per direction, directions in order, so no atomics are needed
     float sacc[NW * WV];
     float saccw[DENS || DW ? NW * WV : 1];
-    float sfoot[NW * Q::NB * FP];
+    alignas(16) float sfoot[NW * Q::NB * FP];
     float sfoot2[DW ? NW * Q::NB * FP : 1];
-    unsigned short squeue[NW * Q::CAP];
+    unsigned char squeue[NW * Q::CAP];
 };
 
 // Bricks of x-width kCBX in row (y brick j, z brick k) that meet the sphere of
@@ -874,7 +879,8 @@ __device__ __forceinline__ void group_sync(int id)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(kCThreads) : "memory");
 }
 
-template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false, bool DEEP = false, int G = kBpGroups>
+template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false, bool DEEP = false, int G = kBpGroups,
+          int TS = 0>
 __global__ void __launch_bounds__(kCThreads *G, G == 1 ? 3 : 1)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
@@ -885,7 +891,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     constexpr int W = ADJ ? 7 : 5, HALF = W / 2;
     using Shape = BpShape<ADJ, DW, DEEP>;
     constexpr int BD = Shape::BD, kWarpVox = Shape::WV, kCBZ = Shape::BZ;
-    constexpr int FW = Shape::FW, FH = FW, FS = FW + 1;
+    constexpr int FW = Shape::FW, FH = FW, FS = FW + (BpQueue<ADJ, DW, DEEP>::NB == 2 ? 4 : 1);
+    // two-buffer form: footprint rows hold the pixels from fi0 & ~3 (16-byte aligned rows)
+    constexpr bool QALIGN = BpQueue<ADJ, DW, DEEP>::NB == 2;
     using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
     // [table: tb.entries x tb.copies][G x Mem][row starts][row prefix]
     extern __shared__ __align__(16) float bp_smem[];
@@ -943,7 +951,8 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         }
         Mem &sm = gmem[grp];
         float *sax = sm.sax;
-        int *slist = sm.slist, *swarp = sm.swarp;
+        unsigned short *slist = sm.slist;
+        int *swarp = sm.swarp;
         const int tid = threadIdx.x - grp * kCThreads, warp = tid >> 5, lane = tid & 31;
         const int x0 = (slo[row] + a - spre[row]) * kCBX, y0 = row * kCBY, z0 = kz * kCBZ;
         const int bx = x0 + (warp & 1) * 8, by = y0 + ((warp >> 1) & 1) * 4, bz = z0 + (warp >> 2) * BD;
@@ -954,7 +963,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         float *const wfoot0 = sm.sfoot + warp * (NB * FH * FS);
         float *const wfoot20 = sm.sfoot2 + (DW ? warp * (NB * FH * FS) : 0);
         BpDirMeta *const wmeta = sm.smeta + warp * NB;
-        unsigned short *const wq = sm.squeue + warp * (QM + 1);
+        unsigned char *const wq = sm.squeue + warp * (QM + 1);
         float *const wacc = sm.sacc + warp * kWarpVox;
         float *const waccw = sm.saccw + (DENS || DW ? warp * kWarpVox : 0);
 
@@ -986,7 +995,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         const float bcx = x0 + 0.5f * (kCBX - 1) - volCenter, bcy = y0 + 0.5f * (kCBY - 1) - volCenter,
                     bcz = z0 + 0.5f * (kCBZ - 1) - volCenter;
         const unsigned lt_mask = (1u << lane) - 1u;
-        int qhead = 0, qsize = 0, nbuf = 0; // the warp's queue (uniform)
+        // the warp's queue (uniform): qsize entries from qhead; the first nfront
+        // belong to footprint buffer bfront, the rest to the other buffer
+        int qhead = 0, qsize = 0, nbuf = 0, nfront = 0, bfront = 0;
 
         // One voxel's window sum for one direction: the fast window from the
         // footprint, or the reference's (or the adjoint's) window from the image.
@@ -1011,9 +1022,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                    (kerCenterHalf - (float)vi * sg) * tb.scale,
                                    (kerCenterHalf - (float)vj * sg) * tb.scale,
                                    (kerCenterHalf - (float)vk * sg) * tb.scale, tb.magic, stride};
-                const float *fb = wfoot + rj * FS + ri;
+                const float *fb = wfoot + rj * FS + ri + (QALIGN ? (fi0 & 3) : 0);
                 const float pi0 = (float)(imgi - HALF - imgCenter), pj0 = (float)(imgj - HALF - imgCenter);
-                foot_window_x2<DENS, W, W, FS, DW>(fwin, fb, tab, pi0, pj0, cs, cw,
+                foot_window_x2<DENS, W, W, FS, DW, TS>(fwin, fb, tab, pi0, pj0, cs, cw,
                                                 DW ? wfoot2 + rj * FS + ri : nullptr);
             } else if (ADJ) {
                 cs = adjoint_window_slow<TI>(vi, vj, vk, volCenter, nx0, nx1, nx2, ny0, ny1, ny2, img_ptr, M,
@@ -1038,16 +1049,15 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             float cs = 0.0f, cw = 0.0f;
             int l = 0, b = 0;
             if (lane < cnt) {
-                const unsigned ent = wq[(qhead + lane) & QM];
-                l = ent & 0xff;
-                b = ent >> 8;
+                l = wq[(qhead + lane) & QM];
+                b = lane < nfront ? bfront : (bfront ^ 1);
                 const BpDirMeta m = wmeta[b];
                 voxel_window(l, m.nx0, m.nx1, m.nx2, m.ny0, m.ny1, m.ny2, m.fi0, m.fj0, m.fh, m.foot != 0,
                              img + (size_t)m.dir * MM, DW ? img2 + (size_t)m.dir * MM : nullptr, wfoot0 + b * (FH * FS),
                              wfoot20 + (DW ? b * (FH * FS) : 0), cs, cw);
             }
             // cumSumAllAxes += cumSum (gpuBackProject.cu:106), in direction order
-            const int bf = wq[qhead & QM] >> 8;
+            const int bf = bfront;
             if (lane < cnt && b == bf) {
                 wacc[l] = __fadd_rn(wacc[l], cs);
                 if (DENS || DW) waccw[l] = __fadd_rn(waccw[l], cw);
@@ -1060,6 +1070,11 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             __syncwarp(); // the entries, buffers and sums are free again
             qhead = (qhead + cnt) & QM;
             qsize -= cnt;
+            nfront -= cnt;
+            if (nfront <= 0) { // the front direction is done: the rest are the other buffer's
+                bfront ^= 1;
+                nfront = qsize;
+            }
         };
 
         for (int c0 = 0; c0 < n; c0 += kBpChunk) {
@@ -1107,7 +1122,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 for (int pss = 0; pss < kPasses; pss++) {
                     int o = off;
                     for (int w = 0; w < warp; w++) o += swarp[pss * (kCThreads / 32) + w];
-                    if (keeps[pss]) slist[o + __popc(ballots[pss] & lt_mask)] = (tid + pss * kCThreads) | orthos[pss];
+                    if (keeps[pss]) slist[o + __popc(ballots[pss] & lt_mask)] = (unsigned short)((tid + pss * kCThreads) | orthos[pss]);
                     for (int w = 0; w < kCThreads / 32; w++) off += swarp[pss * (kCThreads / 32) + w];
                 }
                 if (tid == kCThreads - 1) sm.scount = off;
@@ -1150,7 +1165,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                     b = nbuf;
                     nbuf ^= 1;
                     // buffer b's earlier voxels (all at the front of the queue) run first
-                    while (qsize > 0 && (wq[qhead & QM] >> 8) == b) run_round(min(qsize, 32));
+                    while (qsize > 0 && bfront == b) run_round(min(qsize, 32));
                 }
                 float *const wfoot = wfoot0 + b * (FH * FS);
                 float *const wfoot2 = wfoot20 + (DW ? b * (FH * FS) : 0);
@@ -1195,12 +1210,16 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                         if (DW) v2[e] = __ldg(img2_ptr + lin0 + e);
                                     }
                             }
+                            if (QALIGN) {
+                                *reinterpret_cast<float4 *>(wfoot + r * FS + 4 * qq) = make_float4(v[0], v[1], v[2], v[3]);
+                            } else {
 #pragma unroll
-                            for (int e = 0; e < 4; e++)
-                                if (c0 + e >= 0 && c0 + e < FW) {
-                                    wfoot[r * FS + c0 + e] = v[e];
-                                    if (DW) wfoot2[r * FS + c0 + e] = v2[e];
-                                }
+                                for (int e = 0; e < 4; e++)
+                                    if (c0 + e >= 0 && c0 + e < FW) {
+                                        wfoot[r * FS + c0 + e] = v[e];
+                                        if (DW) wfoot2[r * FS + c0 + e] = v2[e];
+                                    }
+                            }
                         }
                     } else if (foot && !ADJ && sizeof(TI) == 2 && !ONES && !(M & 1)) {
                         // the same with 4-byte pixel pairs when only 2 divides M
@@ -1219,8 +1238,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                 if (lin0 >= 0 && lin0 < MM) v0 = ld_f32(img_ptr + lin0);
                                 if (lin0 + 1 >= 0 && lin0 + 1 < MM) v1 = ld_f32(img_ptr + lin0 + 1);
                             }
-                            if (c0 >= 0 && c0 < FW) wfoot[r * FS + c0] = v0;
-                            if (c0 + 1 < FW) wfoot[r * FS + c0 + 1] = v1; // c0 + 1 >= 0
+                            const int ash = QALIGN ? (fi0 & 3) : 0;
+                            if (c0 >= 0 && c0 < FW) wfoot[r * FS + c0 + ash] = v0;
+                            if (c0 + 1 < FW) wfoot[r * FS + c0 + 1 + ash] = v1; // c0 + 1 >= 0
                         }
                     } else if (foot && !ADJ) {
                         // the reference's linear-index rule (gpuBackProject.cu:99)
@@ -1232,7 +1252,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                 v = ONES ? 1.0f : ld_f32(img_ptr + lin);
                                 if (DW) v2 = __ldg(img2_ptr + lin);
                             }
-                            wfoot[r * FS + c] = v;
+                            wfoot[r * FS + c + (QALIGN ? (fi0 & 3) : 0)] = v;
                             if (DW) wfoot2[r * FS + c] = v2;
                         }
                     } else if (foot) {
@@ -1256,8 +1276,12 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                     for (int s = 0; s < BD; s++) {
                         const bool act = (actm >> s) & 1u;
                         const unsigned bal = __ballot_sync(0xffffffffu, act);
-                        if (act) wq[(pos + __popc(bal & lt_mask)) & QM] = (unsigned short)((lane + 32 * s) | (b << 8));
+                        if (act) wq[(pos + __popc(bal & lt_mask)) & QM] = (unsigned char)(lane + 32 * s);
                         pos += __popc(bal);
+                    }
+                    if (qsize == 0) {
+                        bfront = b;
+                        nfront = total;
                     }
                     qsize += total;
                     __syncwarp(); // the queue entries, the footprint and its record are complete
@@ -1269,7 +1293,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                     for (int s = 0; s < BD; s++) {
                         const bool act = (actm >> s) & 1u;
                         const unsigned bal = __ballot_sync(0xffffffffu, act);
-                        if (act) wq[pos + __popc(bal & lt_mask)] = (unsigned short)(lane + 32 * s);
+                        if (act) wq[pos + __popc(bal & lt_mask)] = (unsigned char)(lane + 32 * s);
                         pos += __popc(bal);
                     }
                     __syncwarp(); // the voxel list and the footprint are complete
@@ -1317,19 +1341,27 @@ static cudaError_t launch_bp_compact_g(float *vol, const TI *img, const float *k
     const BpTable tb = bp_table(g.ker_size, other, max_copies, limit);
     if (tb.copies == 0) return cudaErrorInvalidValue; // a KB table too long for shared memory
     const size_t dyn = (((size_t)tb.entries * tb.copies + 3) & ~(size_t)3) * sizeof(float) + other;
-    auto kern = bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    if (e != cudaSuccess) return e;
     // quad loads of image rows: 4 | M and the stacks aligned to 4 elements
     const size_t qa = 4 * sizeof(TI);
     const int vec = (g.M % 4 == 0) && ((size_t)img % qa == 0) && (!img2 || (size_t)img2 % 16 == 0) ? 1 : 0;
     // CTA (x, z): bricks run x .. of z-layer z that meet the sphere
     const int run = ((DEEP && G > 1) ? 2 : 1) * G;
     const dim3 grid((unsigned)((bx * by + run - 1) / run), (unsigned)bz);
-    kern<<<grid, kCThreads * G, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size, g.ker_hw,
-                                          bx, by, tb, zero_edges ? 1 : 0, scale, img2, vec);
-    count_launches(1);
-    return cudaGetLastError();
+    // the table stride as a compile-time constant where the copy count gives one
+    auto go = [&](auto kern) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, kCThreads * G, dyn, s>>>(vol, pd, g.V, img, g.M, axes, n, g.mask_radius, ker, g.ker_size,
+                                              g.ker_hw, bx, by, tb, zero_edges ? 1 : 0, scale, img2, vec);
+        count_launches(1);
+        return cudaGetLastError();
+    };
+    if constexpr (G == 1) {
+        if (tb.copies == 1) return go(bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G, 4>);
+    } else {
+        if (tb.copies == 32) return go(bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G, 128>);
+    }
+    return go(bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G, 0>);
 }
 
 template <typename TI, bool ONES, bool DENS = false, bool ADJ = false, bool DW = false, bool DEEP = false>
