@@ -821,15 +821,23 @@ struct BpQueue {
     static constexpr int CAP = NEED <= 128 ? 128 : (NEED <= 256 ? 256 : 512);
 };
 
-// One group's working set in shared memory (after the table).
-template <bool DENS, bool ADJ, bool DW, bool DEEP>
+// One group's working set in shared memory (after the table).  LEAN (the
+// launches that own the GPU): 8-bit queue entries with the footprint buffer
+// tracked per warp, 16-bit direction-list entries, and in the two-buffer form
+// footprint rows of FW + 4 pixels from fi0 & ~3 (16-byte aligned, written by
+// vector stores).  Otherwise (the serving lanes' one-group CTAs): 16-bit
+// entries carrying the buffer bit, rows of FW + 1 pixels from fi0.
+template <bool DENS, bool ADJ, bool DW, bool DEEP, bool LEAN = true>
 struct BpGroupMem {
     using Shape = BpShape<ADJ, DW, DEEP>;
     using Q = BpQueue<ADJ, DW, DEEP>;
-    static constexpr int NW = kCThreads / 32, WV = Shape::WV, FP = Shape::FW * (Shape::FW + (Q::NB == 2 ? 4 : 1));
+    using QEnt = typename std::conditional<LEAN, unsigned char, unsigned short>::type;
+    using LEnt = typename std::conditional<LEAN, unsigned short, int>::type;
+    static constexpr int NW = kCThreads / 32, WV = Shape::WV,
+                         FP = Shape::FW * (Shape::FW + (LEAN && Q::NB == 2 ? 4 : 1));
     BpDirMeta smeta[NW * Q::NB];
     float sax[kBpChunk * 9];
-    unsigned short slist[kBpChunk];
+    LEnt slist[kBpChunk];
     int swarp[kBpChunk / 32]; // kept directions per (pass, warp)
     int scount;
     // per-voxel sums [warp][block voxel]; a voxel is updated by at most one
@@ -838,7 +846,7 @@ struct BpGroupMem {
     float saccw[DENS || DW ? NW * WV : 1];
     alignas(16) float sfoot[NW * Q::NB * FP];
     float sfoot2[DW ? NW * Q::NB * FP : 1];
-    unsigned char squeue[NW * Q::CAP];
+    QEnt squeue[NW * Q::CAP];
 };
 
 // Bricks of x-width kCBX in row (y brick j, z brick k) that meet the sphere of
@@ -880,7 +888,7 @@ __device__ __forceinline__ void group_sync(int id)
 }
 
 template <typename TI, bool ONES, bool DENS, bool ADJ, bool DW = false, bool DEEP = false, int G = kBpGroups,
-          int TS = 0>
+          int TS = 0, bool LEAN = true>
 __global__ void __launch_bounds__(kCThreads *G, G == 1 ? 3 : 1)
 bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, const TI *__restrict__ img, int M,
                       const float *__restrict__ axes, int n, int maskR, const float *__restrict__ ker, int kerSize,
@@ -891,10 +899,11 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
     constexpr int W = ADJ ? 7 : 5, HALF = W / 2;
     using Shape = BpShape<ADJ, DW, DEEP>;
     constexpr int BD = Shape::BD, kWarpVox = Shape::WV, kCBZ = Shape::BZ;
-    constexpr int FW = Shape::FW, FH = FW, FS = FW + (BpQueue<ADJ, DW, DEEP>::NB == 2 ? 4 : 1);
-    // two-buffer form: footprint rows hold the pixels from fi0 & ~3 (16-byte aligned rows)
-    constexpr bool QALIGN = BpQueue<ADJ, DW, DEEP>::NB == 2;
-    using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
+    // LEAN two-buffer form: footprint rows hold the pixels from fi0 & ~3 (16-byte aligned rows)
+    constexpr bool QALIGN = LEAN && BpQueue<ADJ, DW, DEEP>::NB == 2;
+    constexpr int FW = Shape::FW, FH = FW, FS = FW + (QALIGN ? 4 : 1);
+    using Mem = BpGroupMem<DENS, ADJ, DW, DEEP, LEAN>;
+    using QEnt = typename Mem::QEnt;
     // [table: tb.entries x tb.copies][G x Mem][row starts][row prefix]
     extern __shared__ __align__(16) float bp_smem[];
     const int cp = tb.copies, tabWords = tb.entries * cp;
@@ -951,7 +960,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         }
         Mem &sm = gmem[grp];
         float *sax = sm.sax;
-        unsigned short *slist = sm.slist;
+        typename Mem::LEnt *slist = sm.slist;
         int *swarp = sm.swarp;
         const int tid = threadIdx.x - grp * kCThreads, warp = tid >> 5, lane = tid & 31;
         const int x0 = (slo[row] + a - spre[row]) * kCBX, y0 = row * kCBY, z0 = kz * kCBZ;
@@ -963,7 +972,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         float *const wfoot0 = sm.sfoot + warp * (NB * FH * FS);
         float *const wfoot20 = sm.sfoot2 + (DW ? warp * (NB * FH * FS) : 0);
         BpDirMeta *const wmeta = sm.smeta + warp * NB;
-        unsigned char *const wq = sm.squeue + warp * (QM + 1);
+        QEnt *const wq = sm.squeue + warp * (QM + 1);
         float *const wacc = sm.sacc + warp * kWarpVox;
         float *const waccw = sm.saccw + (DENS || DW ? warp * kWarpVox : 0);
 
@@ -995,8 +1004,9 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         const float bcx = x0 + 0.5f * (kCBX - 1) - volCenter, bcy = y0 + 0.5f * (kCBY - 1) - volCenter,
                     bcz = z0 + 0.5f * (kCBZ - 1) - volCenter;
         const unsigned lt_mask = (1u << lane) - 1u;
-        // the warp's queue (uniform): qsize entries from qhead; the first nfront
-        // belong to footprint buffer bfront, the rest to the other buffer
+        // the warp's queue (uniform): qsize entries from qhead.  LEAN: the first
+        // nfront belong to footprint buffer bfront, the rest to the other
+        // buffer; otherwise each entry carries its buffer in bit 8
         int qhead = 0, qsize = 0, nbuf = 0, nfront = 0, bfront = 0;
 
         // One voxel's window sum for one direction: the fast window from the
@@ -1049,15 +1059,16 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
             float cs = 0.0f, cw = 0.0f;
             int l = 0, b = 0;
             if (lane < cnt) {
-                l = wq[(qhead + lane) & QM];
-                b = lane < nfront ? bfront : (bfront ^ 1);
+                const unsigned ent = wq[(qhead + lane) & QM];
+                l = ent & 0xff;
+                b = LEAN ? (lane < nfront ? bfront : (bfront ^ 1)) : (int)(ent >> 8);
                 const BpDirMeta m = wmeta[b];
                 voxel_window(l, m.nx0, m.nx1, m.nx2, m.ny0, m.ny1, m.ny2, m.fi0, m.fj0, m.fh, m.foot != 0,
                              img + (size_t)m.dir * MM, DW ? img2 + (size_t)m.dir * MM : nullptr, wfoot0 + b * (FH * FS),
                              wfoot20 + (DW ? b * (FH * FS) : 0), cs, cw);
             }
             // cumSumAllAxes += cumSum (gpuBackProject.cu:106), in direction order
-            const int bf = bfront;
+            const int bf = LEAN ? bfront : (int)(wq[qhead & QM] >> 8);
             if (lane < cnt && b == bf) {
                 wacc[l] = __fadd_rn(wacc[l], cs);
                 if (DENS || DW) waccw[l] = __fadd_rn(waccw[l], cw);
@@ -1122,7 +1133,8 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 for (int pss = 0; pss < kPasses; pss++) {
                     int o = off;
                     for (int w = 0; w < warp; w++) o += swarp[pss * (kCThreads / 32) + w];
-                    if (keeps[pss]) slist[o + __popc(ballots[pss] & lt_mask)] = (unsigned short)((tid + pss * kCThreads) | orthos[pss]);
+                    if (keeps[pss])
+                        slist[o + __popc(ballots[pss] & lt_mask)] = (typename Mem::LEnt)((tid + pss * kCThreads) | orthos[pss]);
                     for (int w = 0; w < kCThreads / 32; w++) off += swarp[pss * (kCThreads / 32) + w];
                 }
                 if (tid == kCThreads - 1) sm.scount = off;
@@ -1165,7 +1177,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                     b = nbuf;
                     nbuf ^= 1;
                     // buffer b's earlier voxels (all at the front of the queue) run first
-                    while (qsize > 0 && bfront == b) run_round(min(qsize, 32));
+                    while (qsize > 0 && (LEAN ? bfront : (int)(wq[qhead & QM] >> 8)) == b) run_round(min(qsize, 32));
                 }
                 float *const wfoot = wfoot0 + b * (FH * FS);
                 float *const wfoot2 = wfoot20 + (DW ? b * (FH * FS) : 0);
@@ -1276,7 +1288,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                     for (int s = 0; s < BD; s++) {
                         const bool act = (actm >> s) & 1u;
                         const unsigned bal = __ballot_sync(0xffffffffu, act);
-                        if (act) wq[(pos + __popc(bal & lt_mask)) & QM] = (unsigned char)(lane + 32 * s);
+                        if (act) wq[(pos + __popc(bal & lt_mask)) & QM] = (QEnt)((lane + 32 * s) | (LEAN ? 0 : b << 8));
                         pos += __popc(bal);
                     }
                     if (qsize == 0) {
@@ -1293,7 +1305,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                     for (int s = 0; s < BD; s++) {
                         const bool act = (actm >> s) & 1u;
                         const unsigned bal = __ballot_sync(0xffffffffu, act);
-                        if (act) wq[pos + __popc(bal & lt_mask)] = (unsigned char)(lane + 32 * s);
+                        if (act) wq[pos + __popc(bal & lt_mask)] = (QEnt)(lane + 32 * s);
                         pos += __popc(bal);
                     }
                     __syncwarp(); // the voxel list and the footprint are complete
@@ -1334,7 +1346,9 @@ static cudaError_t launch_bp_compact_g(float *vol, const TI *img, const float *k
 {
     constexpr int kCBZ = BpShape<ADJ, DW, DEEP>::BZ;
     const int bx = (g.V + kCBX - 1) / kCBX, by = (g.V + kCBY - 1) / kCBY, bz = (g.V + kCBZ - 1) / kCBZ;
-    using Mem = BpGroupMem<DENS, ADJ, DW, DEEP>;
+    // one group per CTA (the serving lanes): the non-LEAN layout
+    constexpr bool LEAN = G > 1;
+    using Mem = BpGroupMem<DENS, ADJ, DW, DEEP, LEAN>;
     const size_t other = G * sizeof(Mem) + (2 * (size_t)by + 1) * sizeof(int);
     // one group per CTA: three CTAs an SM (228 KB, 1 KB reserved per CTA)
     const size_t limit = G == 1 ? (size_t)(228 * 1024 / 3 - 1024) : 0;
@@ -1356,12 +1370,10 @@ static cudaError_t launch_bp_compact_g(float *vol, const TI *img, const float *k
         count_launches(1);
         return cudaGetLastError();
     };
-    if constexpr (G == 1) {
-        if (tb.copies == 1) return go(bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G, 4>);
-    } else {
-        if (tb.copies == 32) return go(bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G, 128>);
+    if constexpr (LEAN) {
+        if (tb.copies == 32) return go(bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G, 128, true>);
     }
-    return go(bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G, 0>);
+    return go(bp_ref_compact_kernel<TI, ONES, DENS, ADJ, DW, DEEP, G, 0, LEAN>);
 }
 
 template <typename TI, bool ONES, bool DENS = false, bool ADJ = false, bool DW = false, bool DEEP = false>
