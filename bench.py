@@ -83,13 +83,13 @@ def workload(args, rank=0, world=1):
 
 FLUSH_BYTES = 512 << 20  # untimed write between steps: 4x the 126 MB L2
 
-# From one-launch ncu captures of the fused back projection at 128^3 x 2,
+# From a one-launch ncu capture of the fused back projection at 128^3 x 2,
 # 1,024 directions per launch (profiles/bp_ref_compact_kernel_density_128cubed_1024dirs.md):
-# DRAM bytes (read + write) and L2 bytes per direction, and the fraction of
-# cycles the schedulers issued.
-NCU_BP_DRAM_PER_DIR = 540.3e6 / 1024
-NCU_BP_LTS_PER_DIR = None
-NCU_BP_ISSUE_ACTIVE = 0.715
+# DRAM bytes (read + write) and L2 bytes (lts__t_bytes) per direction, and the
+# fraction of cycles the schedulers issued.
+NCU_BP_DRAM_PER_DIR = 545.8e6 / 1024
+NCU_BP_LTS_PER_DIR = 5.133e9 / 1024
+NCU_BP_ISSUE_ACTIVE = 0.727
 
 
 def sizes(args):
@@ -342,7 +342,7 @@ def run_gb300(args):
     traffic = lts = issue = None
     if dom == "back" and fused and N == 128 and args.precision == "f32":
         traffic = NCU_BP_DRAM_PER_DIR * units_per_launch
-        lts = NCU_BP_LTS_PER_DIR * units_per_launch if NCU_BP_LTS_PER_DIR else None
+        lts = NCU_BP_LTS_PER_DIR * units_per_launch
         issue = NCU_BP_ISSUE_ACTIVE
     roofline = {"bound": "l2", "kernel": dom, "achieved": achieved, "peak": l2.value, "unit": "GB/s",
                 "frac": achieved / l2.value, "peak_source": "measured in this run (gg_measure_l2_read_gbs, best of 10)",
