@@ -57,6 +57,15 @@ def parse():
     ap.add_argument("--serve-closed", type=int, default=200,
                     help="requests in the closed-loop served vs sequential plain-path comparison")
     ap.add_argument("--serve-repeats", type=int, default=5, help="repeats of the closed-loop comparison")
+    ap.add_argument("--serve-quantum-ms", type=float, default=8.0,
+                    help="estimated device time of one chunk of a served request")
+    ap.add_argument("--serve-backlog", type=float, default=2.0,
+                    help="queued work (estimated seconds) beyond which the offered-rate run sheds arrivals")
+    ap.add_argument("--serve-legs", default="closed,offered,load70",
+                    help="serving runs: closed (served vs sequential), offered (the offered rate), "
+                         "load70 (70%% of the capacity the offered run measured, or of --serve-capacity)")
+    ap.add_argument("--serve-capacity", type=float, default=0.0,
+                    help="requests/s taken as the capacity when the offered run is not among the legs")
     ap.add_argument("--no-precision", action="store_true", help="skip the 256^3 storage-precision comparison")
     ap.add_argument("--no-autograd", action="store_true", help="skip the gradient-descent timing")
     ap.add_argument("--no-ctf", action="store_true", help="skip the CTF-corrected reconstruction timing")
@@ -425,7 +434,7 @@ def run_serve(args):
     measured capacity, and a closed-loop comparison with sequential
     plain-path calls (gg_forward_project / gg_back_project + gg_get_cas_volume)."""
     from multigpugridder_gb300 import synthetic
-    from multigpugridder_gb300._lib import check, lib
+    from multigpugridder_gb300._lib import GG_ERR_BUSY, GridderError, check, lib
     from multigpugridder_gb300.serve import Server, pinned_empty
 
     L = lib()
@@ -436,7 +445,8 @@ def run_serve(args):
     pool = [synthetic.quaternion_axes(4096, 1000 + k).astype(np.float32) for k in range(64)]
     axes = {seed: pool[(seed - 1000) % len(pool)] for _, _, _, _, seed in offered}
     vols = [synthetic.blob_volume(N, b, seed=50 + i) for i, (N, b) in enumerate(zip(SERVE_SIZES, SERVE_BLOBS))]
-    srv = Server(lanes=args.serve_lanes)
+    legs = set(args.serve_legs.split(","))
+    srv = Server(lanes=args.serve_lanes, quantum_ms=args.serve_quantum_ms)
     vids = [srv.add_volume(v) for v in vols]
     sizes = [srv.sizes(v) for v in vids]
     rng = np.random.default_rng(7)
@@ -456,11 +466,15 @@ def run_serve(args):
             return srv.submit(vids[si], op, ax, out=fp_out[si][:n * N * N])
         return srv.submit(vids[si], op, ax, images=img_in[si][:n * N * N], out=bp_out[si])
 
-    def open_loop(sched, scale=1.0):
+    def open_loop(sched, scale=1.0, backlog=0.0):
+        """Arrivals at their scheduled times; with a backlog bound, arrivals that
+        find that much work queued are refused (GG_ERR_BUSY) and counted."""
+        srv.set_max_backlog(backlog)
         srv.reset_stats()
         t0 = time.perf_counter()
-        hs = []
-        for t, si, op, n, seed in sched:
+        hs, kept = [], []
+        for req in sched:
+            t, si, op, n, seed = req
             t = t * scale
             while True:
                 dt = t - (time.perf_counter() - t0)
@@ -468,22 +482,29 @@ def run_serve(args):
                     break
                 if dt > 2e-3:
                     time.sleep(dt - 1e-3)
-            hs.append(submit(si, op, n, seed))
+            try:
+                hs.append(submit(si, op, n, seed))
+                kept.append(req)
+            except GridderError as e:
+                if e.code != GG_ERR_BUSY:
+                    raise
         lats = [srv.wait(h)[1] for h in hs]
         el = time.perf_counter() - t0
+        srv.set_max_backlog(0.0)
         st = srv.stats()
-        dirs = sum(x[3] for x in sched)
+        dirs = sum(x[3] for x in kept)
         # latency percentiles per request class: small (n < 256) and large (n >= 1024)
         # requests on 64^3/128^3 and on 192^3/256^3 volumes
         classes = {}
-        for (t, si, op, n, seed), lat in zip(sched, lats):
+        for (t, si, op, n, seed), lat in zip(kept, lats):
             key = "%s_%s" % ("vol64_128" if si < 2 else "vol192_256",
                              "n_lt_256" if n < 256 else ("n_ge_1024" if n >= 1024 else "n_256_1023"))
             classes.setdefault(key, []).append(lat)
         by_class = {k: {"requests": len(v), "p50_ms": float(np.percentile(v, 50)),
                         "p99_ms": float(np.percentile(v, 99))} for k, v in sorted(classes.items())}
-        return {"offered_rps": len(sched) / (sched[-1][0] * scale) if sched else 0.0, "requests": len(sched),
-                "seconds": el, "throughput_rps": len(sched) / el, "directions_per_s": dirs / el,
+        return {"offered_rps": len(sched) / (sched[-1][0] * scale) if sched else 0.0, "offered": len(sched),
+                "requests": len(kept), "refused": len(sched) - len(kept), "backlog_bound_s": backlog,
+                "seconds": el, "throughput_rps": len(kept) / el, "directions_per_s": dirs / el,
                 "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
                 "peak_inflight": st["peak_inflight"], "peak_gb": st["peak_gb"], "by_class": by_class}
 
@@ -529,27 +550,37 @@ def run_serve(args):
 
     # alternate the two arms so that drifts of the shared GPU hit both alike
     served_runs, seq_runs = [], []
-    for _ in range(max(1, args.serve_repeats)):
-        served_runs.append(served_once())
-        seq_runs.append(sequential_once())
+    if "closed" in legs:
+        for _ in range(max(1, args.serve_repeats)):
+            served_runs.append(served_once())
+            seq_runs.append(sequential_once())
     for h in grids:
         L.gg_destroy(h)
 
-    res_offered = open_loop(offered)
-    cap = res_offered["throughput_rps"]
-    rate70 = 0.7 * min(cap, args.serve_rate)
-    res_70 = open_loop(offered[:max(1, int(rate70 * args.serve_seconds))], scale=args.serve_rate / rate70)
+    res_offered = res_70 = None
+    cap = args.serve_capacity
+    if "offered" in legs:
+        # ten times what one GPU serves: the backlog bound sheds what cannot be
+        # served within about that many seconds, as an overloaded server does
+        res_offered = open_loop(offered, backlog=args.serve_backlog)
+        cap = res_offered["throughput_rps"]
+    if "load70" in legs and cap > 0:
+        rate70 = 0.7 * min(cap, args.serve_rate)
+        res_70 = open_loop(offered[:max(1, int(rate70 * args.serve_seconds))], scale=args.serve_rate / rate70)
     srv.close()
+    closed_res = None
+    if served_runs:
+        closed_res = {"requests": len(closed), "repeats": len(served_runs),
+                      "served_rps": statistics.median(served_runs),
+                      "sequential_plain_rps": statistics.median(seq_runs),
+                      "speedup": statistics.median(a / b for a, b in zip(served_runs, seq_runs)),
+                      "served_rps_runs": served_runs, "sequential_plain_rps_runs": seq_runs}
     return {"workload": "Poisson arrivals at %g req/s for %g s: forwardProject/backProject 50/50 on resident FP32 "
                         "volumes 64^3/128^3/192^3/256^3 (weights .4/.3/.2/.1, interpFactor 2), directions "
                         "log-uniform 16-4096 (random quaternions); back requests return the CAS volume"
                         % (args.serve_rate, args.serve_seconds),
-            "lanes": args.serve_lanes, "offered": res_offered, "at_70pct_capacity": res_70,
-            "closed_loop": {"requests": len(closed), "repeats": len(served_runs),
-                            "served_rps": statistics.median(served_runs),
-                            "sequential_plain_rps": statistics.median(seq_runs),
-                            "speedup": statistics.median(a / b for a, b in zip(served_runs, seq_runs)),
-                            "served_rps_runs": served_runs, "sequential_plain_rps_runs": seq_runs}}
+            "lanes": args.serve_lanes, "quantum_ms": args.serve_quantum_ms, "offered": res_offered,
+            "at_70pct_capacity": res_70, "capacity_rps": cap, "closed_loop": closed_res}
 
 
 # ---- storage precision at 256^3 ------------------------------------------------

@@ -43,6 +43,7 @@ extern "C" {
 #define GG_ERR_NO_DEVICE 5
 #define GG_ERR_CUFFT 6
 #define GG_ERR_TIMEOUT 7 /* gg_server_wait: the request is not done yet */
+#define GG_ERR_BUSY 8    /* gg_server_submit: the backlog bound is reached; retry later */
 
 /* storage precision of the resident CAS volume and of the CAS images the
    projection kernels read (window accumulation is always FP32) */
@@ -304,12 +305,17 @@ int gg_profile_read(gg_gridder *h, int kernel, double *total_ms, long long *laun
  * (MultiGPUGridder.cpp ForwardProject/BackProject).  A server keeps CAS
  * volumes resident (each prepared once, as setVolume does) and runs forward and
  * back projection requests of any volume size and orientation count on
- * `lanes` CUDA streams: a queued request starts as soon as a lane is free and
- * its device buffers fit the HBM budget (FIFO admission by footprint), so the
- * work of requests that arrive while others run overlaps on the device.  A
- * request's result does not depend on what else runs (same kernels, same
- * order).  Host buffers should be pinned (cudaHostAlloc) for the copies to
- * overlap; they must stay valid until gg_server_wait returns.
+ * `lanes` lanes (CUDA stream pairs).  Requests run in chunks of directions of
+ * about one quantum of estimated device time; a free lane takes the chunk of
+ * the request with the least estimated work left (less 0.2 s per second
+ * waited); requests of one quantum or less run on high-priority streams and
+ * have a quarter of the lanes to themselves.
+ * A request starts once its device buffers fit the HBM budget (admission by
+ * footprint, in that order), so the work of requests that arrive while others
+ * run overlaps on the device.  A request's result does not depend on what
+ * else runs (same kernels on the same chunks, in order).  Host buffers should
+ * be pinned (cudaHostAlloc) for the copies to overlap; they must stay valid
+ * until gg_server_wait returns.
  * ------------------------------------------------------------------------- */
 typedef struct gg_server gg_server;
 
@@ -340,6 +346,20 @@ int gg_server_wait(gg_server *s, long long request_id, double timeout_s, double 
 int gg_server_stats(gg_server *s, long long *completed, double *p50_ms, double *p99_ms, double *mean_ms,
                     long long *peak_inflight, double *peak_gb);
 int gg_server_reset_stats(gg_server *s);
+/* Estimated device time of one chunk (default 8 ms).  Smaller quanta let short
+   requests overtake long ones sooner; larger ones cost fewer launches.  It
+   applies to requests submitted afterwards, and fixes how they are chunked
+   (and so the order of a back projection's sums). */
+int gg_server_set_quantum(gg_server *s, double quantum_ms);
+/* Bound on the estimated device time of the requests queued and not yet
+   started; a submission beyond it fails with GG_ERR_BUSY.  0 (the default):
+   no bound. */
+int gg_server_set_max_backlog(gg_server *s, double seconds);
+/* Requests queued (not started) and admitted (started, not done), the
+   estimated seconds of queued work, and the submissions refused with
+   GG_ERR_BUSY since the last reset (each pointer nullable). */
+int gg_server_load(gg_server *s, long long *queued, long long *active, double *queued_seconds,
+                   long long *rejected);
 
 }
 #endif

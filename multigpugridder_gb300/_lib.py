@@ -19,6 +19,7 @@ GG_ERR_STATE = 4
 GG_ERR_NO_DEVICE = 5
 GG_ERR_CUFFT = 6
 GG_ERR_TIMEOUT = 7
+GG_ERR_BUSY = 8
 
 GG_OP_FORWARD = 0
 GG_OP_BACK = 1
@@ -113,6 +114,10 @@ SIGNATURES = {
     "gg_server_stats": (_c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), _dp, _dp, _dp, ctypes.POINTER(ctypes.c_longlong),
                                  _dp]),
     "gg_server_reset_stats": (_c_int, [_vp]),
+    "gg_server_set_quantum": (_c_int, [_vp, ctypes.c_double]),
+    "gg_server_set_max_backlog": (_c_int, [_vp, ctypes.c_double]),
+    "gg_server_load": (_c_int, [_vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong), _dp,
+                                ctypes.POINTER(ctypes.c_longlong)]),
     "gg_profile_enable": (_c_int, [_vp, _c_int]),
     "gg_profile_read": (_c_int, [_vp, _c_int, _dp, ctypes.POINTER(ctypes.c_longlong)]),
 }

@@ -6,15 +6,29 @@
 // worker thread runs forward and back projection requests of any size and
 // orientation count:
 //
-//   * continuous batching: a request is admitted as soon as a lane (a CUDA
-//     stream with its own cuFFT plans) is free and its device memory fits the
-//     HBM budget, whatever else is running; the requests on different lanes
-//     overlap on the device;
-//   * admission by HBM footprint: every request's buffers (directions,
-//     per-chunk images / spectra / CAS images, and for a back projection a
-//     CAS volume) are counted before it starts, in FIFO order;
-//   * each request's work is the same stream-ordered sequence of the same
-//     kernels whatever else runs, so its result does not depend on the mix.
+//   * continuous batching: a request is split into chunks of directions of
+//     about one quantum of estimated device time (8 ms by default); a lane (a
+//     pair of CUDA streams with its own cuFFT plans) runs one chunk at a time,
+//     and the chunks of different requests on different lanes overlap on the
+//     device.  Requests that arrive while others run start on the next lane
+//     that frees, so a 4,096-direction request on a 256^3 volume holds a
+//     lane for one chunk, not for its whole run;
+//   * scheduling by remaining work: a free lane takes the chunk of the
+//     request with the least estimated work left, less 0.2 s per second it
+//     has waited (so no request waits for ever); requests of one quantum or
+//     less ("short") run on the lanes' high-priority streams, whose blocks
+//     the GPU starts before those of the long requests, and long requests
+//     hold at most all lanes but a quarter, which stay free for short ones;
+//   * admission by HBM footprint: every request's buffers (directions, one
+//     chunk of images / spectra / CAS images, and for a back projection a
+//     CAS volume) are counted before its first chunk, in scheduling order; a
+//     request that does not fit waits, and none behind it is admitted first;
+//   * an optional bound on the queued work (gg_server_set_max_backlog):
+//     beyond it a submission is refused with GG_ERR_BUSY, as an overloaded
+//     server sheds load instead of growing its queue without limit;
+//   * each request's work is the same sequence of the same kernels on the
+//     same chunks whatever else runs, one chunk after the other, so its
+//     result does not depend on the mix.
 //
 // A forward request writes n*N*N images (forwardProject); a back request
 // writes the V^3 CAS volume of its images back-projected into zeros
@@ -24,10 +38,10 @@
 #include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
-#include <deque>
 #include <map>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <tuple>
@@ -81,14 +95,27 @@ int pow2ceil(int x)
     return p;
 }
 
-// Directions per chunk for CAS images of edge M: about 64 M floats of CAS
-// images per chunk, a power of two between 16 and 1024.
-int chunk_for(int M)
+// Directions per chunk that fit the chunk buffers for CAS images of edge M:
+// about 64 M floats of CAS images, a power of two between 16 and 1024.
+int chunk_cap(int M)
 {
     int c = 1024;
     while (c > 16 && (size_t)c * M * M > ((size_t)64 << 20)) c >>= 1;
     return c;
 }
+
+// Estimated device seconds of one direction, for ranking requests and bounding
+// the backlog: one GB300 runs the forward projection with its 2-D stage in
+// about 34 ps and the serving back projection in about 120 ps per CAS-image
+// pixel (2.2 and 7.9 ms per 1,000 directions at M = 256).
+double dir_seconds(int op, int M)
+{
+    return (double)M * M * (op == GG_OP_FORWARD ? 3.4e-11 : 1.2e-10);
+}
+constexpr double kChunkSeconds = 2e-5;  // launches and copies of one chunk
+constexpr double kAging = 0.2;          // seconds of work a request gains per second it waits
+constexpr int kActivePerLane = 4;       // admitted requests at most, per lane
+constexpr int kReserveDiv = 4;          // lanes / kReserveDiv lanes are kept for short requests
 
 struct Volume {
     int id;
@@ -104,20 +131,36 @@ struct Request {
     const float *in;
     float *out;
     GridderView view{};
-    size_t footprint = 0;
-    int chunk = 0;
-    int lane = -1;
+    size_t footprint = 0; // device bytes held from admission to completion
+    int chunk = 0;        // directions per chunk
+    int next = 0;         // first direction of the next chunk
+    double est = 0;       // estimated device seconds of the whole request
+    double key = 0;       // scheduling key: smaller runs first
+    bool admitted = false, started = false, high = false;
+    int lane = -1;        // lane of the chunk in flight
+    // device buffers, allocated by the first chunk and freed by the last
+    float *d_axes = nullptr, *d_cas = nullptr, *d_real = nullptr, *d_img = nullptr, *d_acc = nullptr;
+    cufftComplex *d_spec = nullptr;
+    int *d_order = nullptr;
     int status = GG_OK;
     std::string err;
     double t_submit = 0, t_start = 0, t_done = 0;
-    cudaError_t cuda_status = cudaSuccess; // from the stream callback
-    bool gpu_done = false;                 // set by the stream callback
+    cudaError_t cuda_status = cudaSuccess; // of the chunk in flight, from the stream callback
+    bool gpu_done = false;                 // the chunk in flight has finished (stream callback)
     bool done = false;                     // retired by the worker
 };
 
+struct KeyLess {
+    bool operator()(const Request *a, const Request *b) const
+    {
+        return a->key != b->key ? a->key < b->key : a->id < b->id;
+    }
+};
+
 struct Lane {
-    cudaStream_t s = nullptr;
+    cudaStream_t lo = nullptr, hi = nullptr; // low and high stream priority
     bool busy = false;
+    bool long_chunk = false; // the chunk in flight belongs to a long request
     std::map<std::tuple<int, int, int>, cufftHandle> plans; // (type, M, batch)
     void *work = nullptr;                                   // shared cuFFT work area
     size_t work_bytes = 0;
@@ -134,32 +177,56 @@ struct gg_server {
     int device = 0;
     size_t budget = 0, used = 0, resident = 0, peak_used = 0;
     long long peak_inflight = 0;
+    double quantum = 8e-3;     // estimated seconds of one chunk
+    double max_backlog = 0;    // estimated seconds of queued work; 0: unbounded
+    double queued_work = 0;    // estimated seconds of the queued (not admitted) requests
+    long long rejected = 0;
+    int active = 0;            // admitted, not yet retired
     cudaMemPool_t pool = nullptr;
     std::vector<Lane> lanes;
     std::map<int, Volume> volumes;
     int next_vol = 1;
     long long next_req = 1;
-    std::deque<std::shared_ptr<Request>> queue;
-    std::vector<std::shared_ptr<Request>> running;
-    std::map<long long, std::shared_ptr<Request>> reqs;
+    // by class (index 1: short requests, of one quantum or less; 0: long ones)
+    std::set<Request *, KeyLess> queued[2]; // submitted, not admitted
+    std::set<Request *, KeyLess> ready[2];  // admitted, no chunk in flight
+    int long_busy = 0;                      // lanes running a chunk of a long request
+    std::vector<Request *> inflight;     // a chunk on a lane
+    std::map<long long, std::shared_ptr<Request>> reqs; // until waited for
+    std::map<long long, std::shared_ptr<Request>> live; // until retired
     std::vector<double> latencies; // seconds, completed requests since the last reset
     std::string err;
 };
 
 namespace {
 
-// Footprint and chunking of a request (bytes held on the device while it runs).
-void plan_request(Request &r)
+// Remaining estimated device seconds of a request.
+double remaining(const Request &r)
+{
+    const int left = std::max(r.n - r.next, 0);
+    double t = left * dir_seconds(r.op, r.view.M) + ((left + r.chunk - 1) / r.chunk) * kChunkSeconds;
+    if (r.op == GG_OP_BACK) t += (double)r.view.V * r.view.V * r.view.V * 4 * 2e-11; // zeroing and read-back
+    return t;
+}
+
+// Footprint, chunking and cost of a request.  A chunk is the largest power
+// of two of directions (16 at least) whose estimated time fits the quantum,
+// capped by the chunk buffers and the request's size.
+void plan_request(Request &r, double quantum)
 {
     const GridderView &v = r.view;
     const size_t MM = (size_t)v.M * v.M, NN = (size_t)v.N * v.N, H = (size_t)v.M * (v.M / 2 + 1);
-    r.chunk = std::min(chunk_for(v.M), pow2ceil(std::max(r.n, 1)));
+    int c = 16;
+    while (c < chunk_cap(v.M) && 2 * c * dir_seconds(r.op, v.M) <= quantum) c <<= 1;
+    r.chunk = std::min(c, pow2ceil(std::max(r.n, 1)));
     const size_t b = (size_t)r.chunk;
     size_t bytes = (size_t)std::max(r.n, 1) * 9 * sizeof(float);
-    bytes += b * (MM * sizeof(float) + H * sizeof(cufftComplex) + MM * sizeof(float) + NN * sizeof(float) +
-                  sizeof(int));
+    bytes += b * (MM * sizeof(float) + NN * sizeof(float) + sizeof(int));
+    if (!v.fused_fft) bytes += b * (H * sizeof(cufftComplex) + MM * sizeof(float));
     if (r.op == GG_OP_BACK) bytes += (size_t)v.V * v.V * v.V * sizeof(float);
     r.footprint = bytes;
+    r.est = remaining(r);
+    r.high = r.est <= quantum;
 }
 
 cufftHandle lane_plan(Lane &L, cufftType type, int M, int batch)
@@ -175,7 +242,8 @@ cufftHandle lane_plan(Lane &L, cufftType type, int M, int batch)
     GS_CKF(cufftMakePlanMany(p, 2, dims, nullptr, 1, 0, nullptr, 1, 0, type, batch, &ws));
     if (ws > L.work_bytes) {
         // the lane is idle here (plans are made before work is enqueued)
-        GS_CK(cudaStreamSynchronize(L.s));
+        GS_CK(cudaStreamSynchronize(L.lo));
+        GS_CK(cudaStreamSynchronize(L.hi));
         if (L.work) GS_CK(cudaFree(L.work));
         L.work = nullptr;
         GS_CK(cudaMalloc(&L.work, ws));
@@ -183,7 +251,6 @@ cufftHandle lane_plan(Lane &L, cufftType type, int M, int batch)
         for (auto &kv : L.plans) GS_CKF(cufftSetWorkArea(kv.second, L.work));
     }
     GS_CKF(cufftSetWorkArea(p, L.work));
-    GS_CKF(cufftSetStream(p, L.s));
     L.plans[key] = p;
     return p;
 }
@@ -192,7 +259,7 @@ cufftHandle lane_plan(Lane &L, cufftType type, int M, int batch)
 void warm_plans(gg_server *S, int M)
 {
     for (auto &L : S->lanes)
-        for (int b = 16; b <= chunk_for(M); b <<= 1) {
+        for (int b = 16; b <= chunk_cap(M); b <<= 1) {
             lane_plan(L, CUFFT_C2R, M, b);
             lane_plan(L, CUFFT_R2C, M, b);
         }
@@ -200,7 +267,7 @@ void warm_plans(gg_server *S, int M)
 
 void CUDART_CB on_done(cudaStream_t, cudaError_t status, void *p)
 {
-    // runs on a CUDA callback thread after the request's stream work: no CUDA
+    // runs on a CUDA callback thread after the chunk's stream work: no CUDA
     // calls here; `status` carries any error of that work
     auto *pair = static_cast<std::pair<gg_server *, Request *> *>(p);
     gg_server *S = pair->first;
@@ -222,70 +289,94 @@ template <typename T> T *pool_alloc(gg_server *S, size_t count, cudaStream_t s)
     return (T *)p;
 }
 
-// Enqueues a request's whole pipeline on its lane's stream.
-void enqueue(gg_server *S, Request &r)
+// Hands the request's device buffers to `out` (to be freed with
+// cudaFreeAsync) and clears them.
+void take_buffers(Request &r, std::vector<void *> &out)
+{
+    void *bufs[] = {r.d_acc, r.d_order, r.d_img, r.d_real, r.d_spec, r.d_cas, r.d_axes};
+    for (void *p : bufs)
+        if (p) out.push_back(p);
+    r.d_acc = r.d_cas = r.d_real = r.d_img = r.d_axes = nullptr;
+    r.d_spec = nullptr;
+    r.d_order = nullptr;
+}
+
+void free_buffers(Request &r, cudaStream_t s)
+{
+    std::vector<void *> bufs;
+    take_buffers(r, bufs);
+    for (void *p : bufs) cudaFreeAsync(p, s);
+}
+
+// Enqueues the request's next chunk on its lane: the first chunk also
+// allocates the buffers, uploads the directions and zeroes the accumulator;
+// the last one also reads the accumulator back and frees the buffers.  The
+// chunks of a request run one after another (each starts once the previous
+// one has finished), whichever lanes they land on.
+void enqueue_chunk(gg_server *S, Request &r)
 {
     Lane &L = S->lanes[r.lane];
-    const cudaStream_t s = L.s;
+    const cudaStream_t s = r.high ? L.hi : L.lo;
     const GridderView &v = r.view;
     const size_t MM = (size_t)v.M * v.M, NN = (size_t)v.N * v.N, H = (size_t)v.M * (v.M / 2 + 1);
     const int B = r.chunk;
-    // plans first: making one may synchronise the (idle) lane
-    for (int b = 16; b <= B; b <<= 1) lane_plan(L, r.op == GG_OP_FORWARD ? CUFFT_C2R : CUFFT_R2C, v.M, b);
-
-    float *d_axes = pool_alloc<float>(S, (size_t)std::max(r.n, 1) * 9, s);
-    float *d_cas = pool_alloc<float>(S, MM * B, s);
-    cufftComplex *d_spec = pool_alloc<cufftComplex>(S, H * B, s);
-    float *d_real = pool_alloc<float>(S, MM * B, s);
-    float *d_img = pool_alloc<float>(S, NN * B, s);
-    int *d_order = r.op == GG_OP_FORWARD ? pool_alloc<int>(S, B, s) : nullptr;
-    float *d_acc = nullptr;
     const size_t V3 = (size_t)v.V * v.V * v.V;
-    if (r.n > 0) GS_CK(cudaMemcpyAsync(d_axes, r.axes, (size_t)r.n * 9 * sizeof(float), cudaMemcpyHostToDevice, s));
-    if (r.op == GG_OP_BACK) {
-        d_acc = pool_alloc<float>(S, V3, s);
-        GS_CK(cudaMemsetAsync(d_acc, 0, V3 * sizeof(float), s));
-    }
-    for (int c0 = 0; c0 < r.n; c0 += B) {
-        const int b = std::min(B, r.n - c0);
-        const cufftHandle p =
-            v.fused_fft ? 0 : lane_plan(L, r.op == GG_OP_FORWARD ? CUFFT_C2R : CUFFT_R2C, v.M, pow2ceil(b));
-        if (r.op == GG_OP_FORWARD) {
-            GS_CK(launch_forward_project(v.cas, kF32, v.V, d_cas, v.ker, d_axes + (size_t)c0 * 9, b, v.g, v.five_taps,
-                                         nullptr, s, v.cas_y, v.cas_z, d_order));
-            if (v.fused_fft) {
-                GS_CK(launch_cas_to_images_fused(d_cas, v.M, v.N, b, d_img, s));
-            } else {
-                GS_CK(launch_cas_images_to_spectrum(d_cas, v.M, b, d_spec, s));
-                GS_CKF(cufftExecC2R(p, d_spec, d_real));
-                GS_CK(launch_fft_output_to_images(d_real, v.M, v.N, b, d_img, s));
-            }
-            GS_CK(cudaMemcpyAsync(r.out + (size_t)c0 * NN, d_img, (size_t)b * NN * sizeof(float),
-                                  cudaMemcpyDeviceToHost, s));
-        } else {
-            GS_CK(cudaMemcpyAsync(d_img, r.in + (size_t)c0 * NN, (size_t)b * NN * sizeof(float),
-                                  cudaMemcpyHostToDevice, s));
-            if (v.fused_fft) {
-                GS_CK(launch_images_to_cas_fused(d_img, v.N, v.M, b, d_cas, kF32, false, s));
-            } else {
-                GS_CK(launch_images_to_fft_input(d_img, v.N, v.M, b, d_real, s));
-                GS_CKF(cufftExecR2C(p, d_real, d_spec));
-                GS_CK(launch_spectrum_to_cas_images(d_spec, v.M, b, d_cas, kF32, nullptr, s));
-            }
-            GS_CK(launch_back_project_ref(d_acc, d_cas, kF32, false, v.ker, d_axes + (size_t)c0 * 9, b, v.g, nullptr,
-                                          s, true));
+    if (!r.started) {
+        r.started = true;
+        r.d_axes = pool_alloc<float>(S, (size_t)std::max(r.n, 1) * 9, s);
+        r.d_cas = pool_alloc<float>(S, MM * B, s);
+        r.d_img = pool_alloc<float>(S, NN * B, s);
+        if (!v.fused_fft) {
+            r.d_spec = pool_alloc<cufftComplex>(S, H * B, s);
+            r.d_real = pool_alloc<float>(S, MM * B, s);
+        }
+        if (r.op == GG_OP_FORWARD) r.d_order = pool_alloc<int>(S, B, s);
+        if (r.n > 0)
+            GS_CK(cudaMemcpyAsync(r.d_axes, r.axes, (size_t)r.n * 9 * sizeof(float), cudaMemcpyHostToDevice, s));
+        if (r.op == GG_OP_BACK) {
+            r.d_acc = pool_alloc<float>(S, V3, s);
+            GS_CK(cudaMemsetAsync(r.d_acc, 0, V3 * sizeof(float), s));
         }
     }
-    if (r.op == GG_OP_BACK) {
-        GS_CK(cudaMemcpyAsync(r.out, d_acc, V3 * sizeof(float), cudaMemcpyDeviceToHost, s));
-        GS_CK(cudaFreeAsync(d_acc, s));
+    const int c0 = r.next;
+    const int b = std::min(B, r.n - c0);
+    if (b > 0) {
+        cufftHandle p = 0;
+        if (!v.fused_fft) {
+            p = lane_plan(L, r.op == GG_OP_FORWARD ? CUFFT_C2R : CUFFT_R2C, v.M, pow2ceil(b));
+            GS_CKF(cufftSetStream(p, s));
+        }
+        const float *axes = r.d_axes + (size_t)c0 * 9;
+        if (r.op == GG_OP_FORWARD) {
+            GS_CK(launch_forward_project(v.cas, kF32, v.V, r.d_cas, v.ker, axes, b, v.g, v.five_taps, nullptr, s,
+                                         v.cas_y, v.cas_z, r.d_order));
+            if (v.fused_fft) {
+                GS_CK(launch_cas_to_images_fused(r.d_cas, v.M, v.N, b, r.d_img, s));
+            } else {
+                GS_CK(launch_cas_images_to_spectrum(r.d_cas, v.M, b, r.d_spec, s));
+                GS_CKF(cufftExecC2R(p, r.d_spec, r.d_real));
+                GS_CK(launch_fft_output_to_images(r.d_real, v.M, v.N, b, r.d_img, s));
+            }
+            GS_CK(cudaMemcpyAsync(r.out + (size_t)c0 * NN, r.d_img, (size_t)b * NN * sizeof(float),
+                                  cudaMemcpyDeviceToHost, s));
+        } else {
+            GS_CK(cudaMemcpyAsync(r.d_img, r.in + (size_t)c0 * NN, (size_t)b * NN * sizeof(float),
+                                  cudaMemcpyHostToDevice, s));
+            if (v.fused_fft) {
+                GS_CK(launch_images_to_cas_fused(r.d_img, v.N, v.M, b, r.d_cas, kF32, false, s));
+            } else {
+                GS_CK(launch_images_to_fft_input(r.d_img, v.N, v.M, b, r.d_real, s));
+                GS_CKF(cufftExecR2C(p, r.d_real, r.d_spec));
+                GS_CK(launch_spectrum_to_cas_images(r.d_spec, v.M, b, r.d_cas, kF32, nullptr, s));
+            }
+            GS_CK(launch_back_project_ref(r.d_acc, r.d_cas, kF32, false, v.ker, axes, b, v.g, nullptr, s, true));
+        }
     }
-    if (d_order) GS_CK(cudaFreeAsync(d_order, s));
-    GS_CK(cudaFreeAsync(d_img, s));
-    GS_CK(cudaFreeAsync(d_real, s));
-    GS_CK(cudaFreeAsync(d_spec, s));
-    GS_CK(cudaFreeAsync(d_cas, s));
-    GS_CK(cudaFreeAsync(d_axes, s));
+    r.next = c0 + std::max(b, 0);
+    if (r.next >= r.n) {
+        if (r.op == GG_OP_BACK) GS_CK(cudaMemcpyAsync(r.out, r.d_acc, V3 * sizeof(float), cudaMemcpyDeviceToHost, s));
+        free_buffers(r, s);
+    }
     auto *arg = new std::pair<gg_server *, Request *>(S, &r);
     cudaError_t e = cudaStreamAddCallback(s, on_done, arg, 0);
     if (e != cudaSuccess) {
@@ -294,42 +385,72 @@ void enqueue(gg_server *S, Request &r)
     }
 }
 
-// Marks a finished request done and returns its resources (lock held).
-void retire(gg_server *S, Request &r)
+// Marks a request done and returns its resources (lock held).  A failed
+// request may still hold device buffers (its lane has drained): they go to
+// `frees`, for cudaFreeAsync once the lock is released.
+void retire(gg_server *S, Request *r, std::vector<std::pair<void *, cudaStream_t>> &frees)
 {
-    if (r.cuda_status != cudaSuccess && r.status == GG_OK) {
-        r.status = GG_ERR_CUDA;
-        r.err = cudaGetErrorString(r.cuda_status);
+    if (r->lane >= 0) {
+        std::vector<void *> bufs;
+        take_buffers(*r, bufs);
+        for (void *p : bufs) frees.emplace_back(p, S->lanes[r->lane].lo);
     }
-    r.done = true;
-    S->lanes[r.lane].busy = false;
-    S->used -= r.footprint;
-    auto vit = S->volumes.find(r.vol_id);
+    if (r->admitted) {
+        S->used -= r->footprint;
+        S->active--;
+    }
+    r->done = true;
+    auto vit = S->volumes.find(r->vol_id);
     if (vit != S->volumes.end()) vit->second.refs--;
-    if (r.status == GG_OK) S->latencies.push_back(r.t_done - r.t_submit);
+    if (r->status == GG_OK) S->latencies.push_back(r->t_done - r->t_submit);
+    S->live.erase(r->id);
 }
 
 void worker_main(gg_server *S)
 {
     cudaSetDevice(S->device);
     std::unique_lock<std::mutex> lk(S->mu);
+    std::vector<std::pair<void *, cudaStream_t>> frees;
     for (;;) {
         bool progress = false;
-        // retire requests whose stream work has finished
-        for (size_t i = 0; i < S->running.size();) {
-            Request &r = *S->running[i];
-            if (!r.gpu_done) {
+        // chunks whose stream work has finished
+        for (size_t i = 0; i < S->inflight.size();) {
+            Request *r = S->inflight[i];
+            if (!r->gpu_done) {
                 i++;
                 continue;
             }
-            retire(S, r);
-            S->running.erase(S->running.begin() + i);
+            S->inflight.erase(S->inflight.begin() + i);
+            Lane &L = S->lanes[r->lane];
+            L.busy = false;
+            if (L.long_chunk) S->long_busy--;
+            L.long_chunk = false;
+            r->gpu_done = false;
+            if (r->cuda_status != cudaSuccess && r->status == GG_OK) {
+                r->status = GG_ERR_CUDA;
+                r->err = cudaGetErrorString(r->cuda_status);
+            }
+            if (r->status != GG_OK || r->next >= r->n) {
+                retire(S, r, frees);
+            } else {
+                r->key = remaining(*r) + kAging * r->t_submit;
+                S->ready[r->high].insert(r);
+            }
             progress = true;
         }
         if (progress) S->cv_done.notify_all();
-        // admit in arrival order while a lane is free and the footprint fits
-        while (!S->queue.empty() && !S->paused) {
-            auto r = S->queue.front();
+        if (!frees.empty()) {
+            lk.unlock();
+            for (auto &f : frees) cudaFreeAsync(f.first, f.second);
+            lk.lock();
+            frees.clear();
+        }
+        // a free lane runs the chunk of the request with the least remaining
+        // work (less kAging per second it has waited), admitted or not; long
+        // requests fill at most all lanes but lanes / kReserveDiv, which stay
+        // free for short ones.  A request whose footprint does not fit waits
+        // for memory, and no request with a larger key is admitted before it.
+        while (!S->paused) {
             int lane = -1;
             for (size_t i = 0; i < S->lanes.size(); i++)
                 if (!S->lanes[i].busy) {
@@ -337,37 +458,59 @@ void worker_main(gg_server *S)
                     break;
                 }
             if (lane < 0) break;
-            if (S->resident + r->footprint > S->budget) {
-                S->queue.pop_front();
-                r->status = GG_ERR_OUT_OF_MEMORY;
-                r->err = "request footprint exceeds the server's HBM budget";
-                r->done = true;
-                r->t_done = now_s();
-                auto vit = S->volumes.find(r->vol_id);
-                if (vit != S->volumes.end()) vit->second.refs--;
-                S->cv_done.notify_all();
-                continue;
+            for (auto &qs : S->queued)
+                while (!qs.empty() && S->resident + (*qs.begin())->footprint > S->budget) {
+                    Request *x = *qs.begin();
+                    qs.erase(qs.begin());
+                    S->queued_work -= x->est;
+                    x->status = GG_ERR_OUT_OF_MEMORY;
+                    x->err = "request footprint exceeds the server's HBM budget";
+                    x->t_done = now_s();
+                    retire(S, x, frees);
+                    S->cv_done.notify_all();
+                }
+            const int nl = (int)S->lanes.size();
+            const bool long_ok = S->long_busy < nl - nl / kReserveDiv;
+            auto best = [&](std::set<Request *, KeyLess> *sets) {
+                Request *x = sets[1].empty() ? nullptr : *sets[1].begin();
+                if (long_ok && !sets[0].empty() && (!x || KeyLess()(*sets[0].begin(), x))) x = *sets[0].begin();
+                return x;
+            };
+            Request *q = best(S->queued), *a = best(S->ready);
+            const bool admit = q && (!a || KeyLess()(q, a)) &&
+                               S->resident + S->used + q->footprint <= S->budget &&
+                               S->active < kActivePerLane * nl;
+            Request *r = admit ? q : a;
+            if (!r) break;
+            if (admit) {
+                S->queued[r->high].erase(r);
+                S->queued_work -= r->est;
+                r->admitted = true;
+                S->used += r->footprint;
+                S->active++;
+                S->peak_used = std::max(S->peak_used, S->resident + S->used);
+                S->peak_inflight = std::max<long long>(S->peak_inflight, S->active);
+                r->t_start = now_s();
+            } else {
+                S->ready[r->high].erase(r);
             }
-            if (S->resident + S->used + r->footprint > S->budget) break;
-            S->queue.pop_front();
+            if (!r->high) {
+                S->lanes[lane].long_chunk = true;
+                S->long_busy++;
+            }
             r->lane = lane;
             S->lanes[lane].busy = true;
-            S->used += r->footprint;
-            S->peak_used = std::max(S->peak_used, S->resident + S->used);
-            r->t_start = now_s();
-            S->running.push_back(r);
-            S->peak_inflight = std::max<long long>(S->peak_inflight, (long long)S->running.size());
+            S->inflight.push_back(r);
             lk.unlock();
             try {
-                enqueue(S, *r);
+                enqueue_chunk(S, *r);
             } catch (const ServeError &e) {
+                // what was enqueued still runs; the request retires once its lane drains
+                cudaStreamSynchronize(S->lanes[lane].lo);
+                cudaStreamSynchronize(S->lanes[lane].hi);
                 lk.lock();
                 r->status = e.code;
                 r->err = e.msg;
-                // what was enqueued still runs; the request retires when the lane drains
-                lk.unlock();
-                cudaStreamSynchronize(S->lanes[lane].s);
-                lk.lock();
                 r->t_done = now_s();
                 r->gpu_done = true;
                 lk.unlock();
@@ -375,7 +518,7 @@ void worker_main(gg_server *S)
             lk.lock();
             progress = true;
         }
-        if (S->stop && S->queue.empty() && S->running.empty()) break;
+        if (S->stop && S->queued[0].empty() && S->queued[1].empty() && S->active == 0 && S->inflight.empty()) break;
         if (!progress) S->cv_work.wait(lk);
     }
 }
@@ -429,8 +572,13 @@ extern "C" int gg_server_create(int device, double hbm_budget_gb, int lanes, gg_
         GS_CK(cudaMemPoolCreate(&S->pool, &props));
         uint64_t keep = UINT64_MAX; // keep freed blocks for reuse
         GS_CK(cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        int least = 0, greatest = 0;
+        GS_CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
         S->lanes.resize(lanes);
-        for (auto &L : S->lanes) GS_CK(cudaStreamCreateWithFlags(&L.s, cudaStreamNonBlocking));
+        for (auto &L : S->lanes) {
+            GS_CK(cudaStreamCreateWithPriority(&L.lo, cudaStreamNonBlocking, least));
+            GS_CK(cudaStreamCreateWithPriority(&L.hi, cudaStreamNonBlocking, greatest));
+        }
     } catch (const ServeError &e) {
         set_global_error(e.msg.c_str());
         gg_server_destroy(S);
@@ -454,10 +602,12 @@ extern "C" void gg_server_destroy(gg_server *S)
     }
     cudaSetDevice(S->device);
     for (auto &L : S->lanes) {
-        if (L.s) cudaStreamSynchronize(L.s);
+        if (L.lo) cudaStreamSynchronize(L.lo);
+        if (L.hi) cudaStreamSynchronize(L.hi);
         for (auto &kv : L.plans) cufftDestroy(kv.second);
         if (L.work) cudaFree(L.work);
-        if (L.s) cudaStreamDestroy(L.s);
+        if (L.lo) cudaStreamDestroy(L.lo);
+        if (L.hi) cudaStreamDestroy(L.hi);
     }
     for (auto &kv : S->volumes) gg_destroy(kv.second.h);
     if (S->pool) cudaMemPoolDestroy(S->pool);
@@ -498,7 +648,7 @@ extern "C" int gg_server_add_volume(gg_server *S, const float *volume, int volum
         {   // hold admission and let the lanes drain: plans are made on idle lanes
             std::unique_lock<std::mutex> lk(S->mu);
             S->paused++;
-            S->cv_done.wait(lk, [&] { return S->running.empty(); });
+            S->cv_done.wait(lk, [&] { return S->inflight.empty(); });
         }
         try {
             warm_plans(S, v.view.M);
@@ -570,12 +720,20 @@ extern "C" int gg_server_submit(gg_server *S, int volume_id, int op, const float
             auto it = S->volumes.find(volume_id);
             if (it == S->volumes.end()) sfail(GG_ERR_INVALID_ARG, "unknown volume id %d", volume_id);
             r->view = it->second.view;
-            plan_request(*r);
+            plan_request(*r, S->quantum);
+            if (S->max_backlog > 0 && S->queued_work >= S->max_backlog) {
+                S->rejected++;
+                sfail(GG_ERR_BUSY, "the server's backlog is full (%.3f s of queued work); retry later",
+                      S->queued_work);
+            }
             it->second.refs++;
             r->id = S->next_req++;
             r->t_submit = now_s();
+            r->key = r->est + kAging * r->t_submit;
             S->reqs[r->id] = r;
-            S->queue.push_back(r);
+            S->live[r->id] = r;
+            S->queued[r->high].insert(r.get());
+            S->queued_work += r->est;
             *request_id = r->id;
         }
         S->cv_work.notify_all();
@@ -636,7 +794,38 @@ extern "C" int gg_server_reset_stats(gg_server *S)
     return sguard(S, [&] {
         std::lock_guard<std::mutex> lock(S->mu);
         S->latencies.clear();
-        S->peak_inflight = (long long)S->running.size();
+        S->peak_inflight = S->active;
         S->peak_used = S->resident + S->used;
+        S->rejected = 0;
+    });
+}
+
+extern "C" int gg_server_set_quantum(gg_server *S, double quantum_ms)
+{
+    return sguard(S, [&] {
+        if (!(quantum_ms > 0)) sfail(GG_ERR_INVALID_ARG, "quantum_ms must be > 0");
+        std::lock_guard<std::mutex> lock(S->mu);
+        S->quantum = quantum_ms * 1e-3;
+    });
+}
+
+extern "C" int gg_server_set_max_backlog(gg_server *S, double seconds)
+{
+    return sguard(S, [&] {
+        if (!(seconds >= 0)) sfail(GG_ERR_INVALID_ARG, "the backlog bound must be >= 0 seconds");
+        std::lock_guard<std::mutex> lock(S->mu);
+        S->max_backlog = seconds;
+    });
+}
+
+extern "C" int gg_server_load(gg_server *S, long long *queued, long long *active, double *queued_seconds,
+                              long long *rejected)
+{
+    return sguard(S, [&] {
+        std::lock_guard<std::mutex> lock(S->mu);
+        if (queued) *queued = (long long)(S->queued[0].size() + S->queued[1].size());
+        if (active) *active = S->active;
+        if (queued_seconds) *queued_seconds = S->queued_work;
+        if (rejected) *rejected = S->rejected;
     });
 }

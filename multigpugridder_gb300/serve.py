@@ -6,10 +6,13 @@
     images, latency_ms = srv.wait(req)                   # n x N x N
 
 A back request returns the V^3 CAS volume of its images back-projected into
-zeros.  Requests run on `lanes` CUDA streams as soon as a lane is free and
-their device buffers fit the HBM budget; requests that arrive while others run
-overlap with them.  For copies that overlap, pass pinned host buffers
-(`pinned_empty`).
+zeros.  Requests run in chunks of about `quantum_ms` of device time on `lanes`
+lanes; a free lane takes the chunk of the request with the least work left, and
+a request starts once its device buffers fit the HBM budget, so requests that
+arrive while others run overlap with them and short ones overtake long ones.
+With `max_backlog_s` set, a submission beyond that much queued work raises
+GridderError with code GG_ERR_BUSY.  For copies that overlap, pass pinned host
+buffers (`pinned_empty`).
 """
 import ctypes
 
@@ -40,7 +43,7 @@ class Request:
 
 
 class Server:
-    def __init__(self, device=0, hbm_budget_gb=0.0, lanes=8):
+    def __init__(self, device=0, hbm_budget_gb=0.0, lanes=8, quantum_ms=None, max_backlog_s=None):
         self._L = _lib.lib()
         h = ctypes.c_void_p()
         rc = self._L.gg_server_create(int(device), float(hbm_budget_gb), int(lanes), ctypes.byref(h))
@@ -48,6 +51,26 @@ class Server:
             raise GridderError(rc, self._L.gg_global_error().decode(errors="replace"))
         self._h = h
         self._sizes = {}
+        if quantum_ms is not None:
+            self.set_quantum(quantum_ms)
+        if max_backlog_s is not None:
+            self.set_max_backlog(max_backlog_s)
+
+    def set_quantum(self, quantum_ms):
+        """Estimated device time of one chunk, for requests submitted afterwards."""
+        self._check(self._L.gg_server_set_quantum(self._h, float(quantum_ms)))
+
+    def set_max_backlog(self, seconds):
+        """Refuse submissions (GG_ERR_BUSY) beyond this much queued work; 0: no bound."""
+        self._check(self._L.gg_server_set_max_backlog(self._h, float(seconds)))
+
+    def load(self):
+        """Requests queued and admitted, seconds of queued work, submissions refused."""
+        q, a, r = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        sec = ctypes.c_double()
+        self._check(self._L.gg_server_load(self._h, ctypes.byref(q), ctypes.byref(a), ctypes.byref(sec),
+                                           ctypes.byref(r)))
+        return {"queued": q.value, "active": a.value, "queued_seconds": sec.value, "rejected": r.value}
 
     def _check(self, rc):
         if rc != GG_OK:

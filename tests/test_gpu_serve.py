@@ -123,3 +123,80 @@ def test_large_volume_equals_plain_path(cuda, gglib):
         fwd = srv.wait(srv.submit(vid, "forward", axes))[0].copy()
     assert O.rel_l2(back, _plain(gglib, v, "back", axes, imgs)) < 1e-6
     assert O.rel_l2(fwd, _plain(gglib, v, "forward", axes, None)) < 1e-6
+
+
+def test_chunked_mix_equals_alone_and_plain_path(cuda, gglib):
+    """A quantum small enough that every request runs in chunks of 16
+    directions, whose chunks of different requests interleave across the
+    lanes: the mix equals the same requests one at a time bit for bit, and the
+    plain gridder calls within relative L2 1e-6 (a chunked back projection sums
+    its chunks' sums in another grouping)."""
+    from multigpugridder_gb300.serve import Server
+
+    vols = {}
+    with Server(lanes=3, quantum_ms=1e-6) as srv:
+        for N, seed in ((16, 81), (24, 82)):
+            v = O.blob_volume(N, 6, seed=seed).astype(np.float32)
+            vols[srv.add_volume(v)] = v
+        reqs = _requests(vols, seed=83, count=16)
+        assert max(len(a) for _, _, a, _ in reqs) > 64
+        handles = [srv.submit(vid, op, axes, imgs) for vid, op, axes, imgs in reqs]
+        mixed = [srv.wait(h)[0].copy() for h in handles]
+        assert srv.stats()["peak_inflight"] > 1
+        alone = [srv.wait(srv.submit(vid, op, axes, imgs))[0].copy() for vid, op, axes, imgs in reqs]
+    for (vid, op, axes, imgs), a, b in zip(reqs, mixed, alone):
+        assert np.array_equal(a, b), (op, len(axes))
+    for k, (vid, op, axes, imgs) in enumerate(reqs):
+        if len(axes) > 32:
+            ref = _plain(gglib, vols[vid], op, axes, imgs)
+            assert O.rel_l2(mixed[k], ref) < 1e-6, (op, len(axes))
+
+
+def test_short_requests_overtake_a_long_one(cuda):
+    """One lane, a long request submitted first and short ones after it: the
+    long request runs in chunks and the short ones, with less work left, take
+    the lane between its chunks and finish first."""
+    from multigpugridder_gb300.serve import Server
+
+    v = O.blob_volume(32, 6, seed=84).astype(np.float32)
+    long_axes = O.quaternion_axes(2048, 85).astype(np.float32)
+    short_axes = O.quaternion_axes(16, 86).astype(np.float32)
+    with Server(lanes=1, quantum_ms=0.01) as srv:
+        vid = srv.add_volume(v)
+        srv.wait(srv.submit(vid, "forward", short_axes))  # plans and kernels warm
+        big = srv.submit(vid, "forward", long_axes)
+        small = [srv.submit(vid, "forward", short_axes) for _ in range(8)]
+        lat_small = [srv.wait(h)[1] for h in small]
+        lat_big = srv.wait(big)[1]
+        ref = srv.wait(srv.submit(vid, "forward", short_axes))[0].copy()
+    assert max(lat_small) < lat_big, (lat_small, lat_big)
+    assert np.all(np.isfinite(ref))
+
+
+def test_backlog_bound_sheds_load(cuda):
+    """With a bound on the queued work, submissions beyond it fail with
+    GG_ERR_BUSY at once, every accepted request completes, and the server
+    keeps serving."""
+    from multigpugridder_gb300 import _lib
+    from multigpugridder_gb300._lib import GridderError
+    from multigpugridder_gb300.serve import Server
+
+    v = O.blob_volume(32, 6, seed=87).astype(np.float32)
+    axes = O.quaternion_axes(512, 88).astype(np.float32)
+    with Server(lanes=1, max_backlog_s=1e-6) as srv:
+        vid = srv.add_volume(v)
+        ok, busy = [], 0
+        for _ in range(64):
+            try:
+                ok.append(srv.submit(vid, "forward", axes))
+            except GridderError as e:
+                assert e.code == _lib.GG_ERR_BUSY
+                busy += 1
+        assert busy > 0 and ok
+        assert srv.load()["rejected"] == busy
+        outs = [srv.wait(h)[0] for h in ok]
+        for o in outs[1:]:
+            assert np.array_equal(o, outs[0])
+        srv.set_max_backlog(0)
+        out, _ = srv.wait(srv.submit(vid, "forward", axes[:5]))
+        assert np.array_equal(out, outs[0][:5])
