@@ -1206,31 +1206,52 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                         // pixel by pixel
                         constexpr int NQ = FW / 4 + 1; // quads per footprint row
                         const int base = fi0 & ~3, sh = fi0 & 3;
-                        for (int t = lane; t < fh * NQ; t += 32) {
-                            const int r = t / NQ, qq = t - r * NQ;
-                            const int c0 = 4 * qq - sh; // footprint column of the quad's first pixel
-                            const int lin0 = (fj0 + r) * M + base + 4 * qq;
-                            float v[4] = {0.0f, 0.0f, 0.0f, 0.0f}, v2[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-                            if (lin0 >= 0 && lin0 + 3 < MM) {
-                                ld_quad(img_ptr + lin0, v);
-                                if (DW) ld_quad(img2_ptr + lin0, v2);
-                            } else {
+                        // a lane's quads (at most KQ) are all loaded before any is
+                        // stored, so their L2 latencies overlap
+                        constexpr int KQ = (FH * NQ + 31) / 32;
+                        const int nq = fh * NQ;
+                        float v[KQ][4], v2[DW ? KQ : 1][4];
 #pragma unroll
-                                for (int e = 0; e < 4; e++)
-                                    if (lin0 + e >= 0 && lin0 + e < MM) {
-                                        v[e] = ld_f32(img_ptr + lin0 + e);
-                                        if (DW) v2[e] = __ldg(img2_ptr + lin0 + e);
-                                    }
+                        for (int u = 0; u < KQ; u++) {
+                            const int t = lane + 32 * u;
+#pragma unroll
+                            for (int e = 0; e < 4; e++) {
+                                v[u][e] = 0.0f;
+                                if (DW) v2[u][e] = 0.0f;
                             }
-                            if (QALIGN) {
-                                *reinterpret_cast<float4 *>(wfoot + r * FS + 4 * qq) = make_float4(v[0], v[1], v[2], v[3]);
-                            } else {
+                            if (t < nq) {
+                                const int r = t / NQ, qq = t - r * NQ;
+                                const int lin0 = (fj0 + r) * M + base + 4 * qq;
+                                if (lin0 >= 0 && lin0 + 3 < MM) {
+                                    ld_quad(img_ptr + lin0, v[u]);
+                                    if (DW) ld_quad(img2_ptr + lin0, v2[DW ? u : 0]);
+                                } else {
 #pragma unroll
-                                for (int e = 0; e < 4; e++)
-                                    if (c0 + e >= 0 && c0 + e < FW) {
-                                        wfoot[r * FS + c0 + e] = v[e];
-                                        if (DW) wfoot2[r * FS + c0 + e] = v2[e];
-                                    }
+                                    for (int e = 0; e < 4; e++)
+                                        if (lin0 + e >= 0 && lin0 + e < MM) {
+                                            v[u][e] = ld_f32(img_ptr + lin0 + e);
+                                            if (DW) v2[DW ? u : 0][e] = __ldg(img2_ptr + lin0 + e);
+                                        }
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int u = 0; u < KQ; u++) {
+                            const int t = lane + 32 * u;
+                            if (t < nq) {
+                                const int r = t / NQ, qq = t - r * NQ;
+                                const int c0 = 4 * qq - sh; // footprint column of the quad's first pixel
+                                if (QALIGN) {
+                                    *reinterpret_cast<float4 *>(wfoot + r * FS + 4 * qq) =
+                                        make_float4(v[u][0], v[u][1], v[u][2], v[u][3]);
+                                } else {
+#pragma unroll
+                                    for (int e = 0; e < 4; e++)
+                                        if (c0 + e >= 0 && c0 + e < FW) {
+                                            wfoot[r * FS + c0 + e] = v[u][e];
+                                            if (DW) wfoot2[r * FS + c0 + e] = v2[DW ? u : 0][e];
+                                        }
+                                }
                             }
                         }
                     } else if (foot && !ADJ && sizeof(TI) == 2 && !ONES && !(M & 1)) {
