@@ -96,9 +96,9 @@ FLUSH_BYTES = 512 << 20  # untimed write between steps: 4x the 126 MB L2
 # 1,024 directions per launch (profiles/bp_ref_compact_kernel_density_128cubed_1024dirs.md):
 # DRAM bytes (read + write) and L2 bytes (lts__t_bytes) per direction, and the
 # fraction of cycles the schedulers issued.
-NCU_BP_DRAM_PER_DIR = 545.8e6 / 1024
-NCU_BP_LTS_PER_DIR = 5.133e9 / 1024
-NCU_BP_ISSUE_ACTIVE = 0.727
+NCU_BP_DRAM_PER_DIR = 545.2e6 / 1024
+NCU_BP_LTS_PER_DIR = 5.488e9 / 1024
+NCU_BP_ISSUE_ACTIVE = 0.720
 
 
 def sizes(args):

@@ -1091,7 +1091,17 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
         for (int c0 = 0; c0 < n; c0 += kBpChunk) {
             const int cn = min(kBpChunk, n - c0);
             group_sync(grp + 1);
-            for (int t = tid; t < cn * 9; t += kCThreads) sax[t] = __ldg(axes + (size_t)c0 * 9 + t);
+            if (cn == kBpChunk) {
+                // a whole chunk: all of a thread's loads in flight before its stores
+                constexpr int KA = kBpChunk * 9 / kCThreads;
+                float a[KA];
+#pragma unroll
+                for (int u = 0; u < KA; u++) a[u] = __ldg(axes + (size_t)c0 * 9 + tid + u * kCThreads);
+#pragma unroll
+                for (int u = 0; u < KA; u++) sax[tid + u * kCThreads] = a[u];
+            } else {
+                for (int t = tid; t < cn * 9; t += kCThreads) sax[t] = __ldg(axes + (size_t)c0 * 9 + t);
+            }
             group_sync(grp + 1);
             // cull: thread tid takes directions tid + p * kCThreads; the kept
             // ones are listed in direction order (pass by pass, warp by warp)
@@ -1206,51 +1216,69 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                         // pixel by pixel
                         constexpr int NQ = FW / 4 + 1; // quads per footprint row
                         const int base = fi0 & ~3, sh = fi0 & 3;
-                        // a lane's quads (at most KQ) are all loaded before any is
-                        // stored, so their L2 latencies overlap
-                        constexpr int KQ = (FH * NQ + 31) / 32;
-                        const int nq = fh * NQ;
-                        float v[KQ][4], v2[DW ? KQ : 1][4];
-#pragma unroll
-                        for (int u = 0; u < KQ; u++) {
-                            const int t = lane + 32 * u;
-#pragma unroll
-                            for (int e = 0; e < 4; e++) {
-                                v[u][e] = 0.0f;
-                                if (DW) v2[u][e] = 0.0f;
-                            }
-                            if (t < nq) {
+                        if constexpr (DW) {
+                            // two image stacks: one quad at a time (both stacks'
+                            // quads held at once would spill)
+                            for (int t = lane; t < fh * NQ; t += 32) {
                                 const int r = t / NQ, qq = t - r * NQ;
+                                const int c0 = 4 * qq - sh; // footprint column of the quad's first pixel
                                 const int lin0 = (fj0 + r) * M + base + 4 * qq;
+                                float v[4] = {0.0f, 0.0f, 0.0f, 0.0f}, v2[4] = {0.0f, 0.0f, 0.0f, 0.0f};
                                 if (lin0 >= 0 && lin0 + 3 < MM) {
-                                    ld_quad(img_ptr + lin0, v[u]);
-                                    if (DW) ld_quad(img2_ptr + lin0, v2[DW ? u : 0]);
+                                    ld_quad(img_ptr + lin0, v);
+                                    ld_quad(img2_ptr + lin0, v2);
                                 } else {
 #pragma unroll
                                     for (int e = 0; e < 4; e++)
                                         if (lin0 + e >= 0 && lin0 + e < MM) {
-                                            v[u][e] = ld_f32(img_ptr + lin0 + e);
-                                            if (DW) v2[DW ? u : 0][e] = __ldg(img2_ptr + lin0 + e);
+                                            v[e] = ld_f32(img_ptr + lin0 + e);
+                                            v2[e] = __ldg(img2_ptr + lin0 + e);
                                         }
                                 }
+#pragma unroll
+                                for (int e = 0; e < 4; e++)
+                                    if (c0 + e >= 0 && c0 + e < FW) {
+                                        wfoot[r * FS + c0 + e] = v[e];
+                                        wfoot2[r * FS + c0 + e] = v2[e];
+                                    }
                             }
-                        }
+                        } else {
+                            // a lane's quads (at most KQ) are all loaded before any is
+                            // stored, so their L2 latencies overlap
+                            constexpr int KQ = (FH * NQ + 31) / 32;
+                            const int nq = fh * NQ;
+                            float v[KQ][4];
 #pragma unroll
-                        for (int u = 0; u < KQ; u++) {
-                            const int t = lane + 32 * u;
-                            if (t < nq) {
-                                const int r = t / NQ, qq = t - r * NQ;
-                                const int c0 = 4 * qq - sh; // footprint column of the quad's first pixel
-                                if (QALIGN) {
-                                    *reinterpret_cast<float4 *>(wfoot + r * FS + 4 * qq) =
-                                        make_float4(v[u][0], v[u][1], v[u][2], v[u][3]);
-                                } else {
+                            for (int u = 0; u < KQ; u++) {
+                                const int t = lane + 32 * u;
 #pragma unroll
-                                    for (int e = 0; e < 4; e++)
-                                        if (c0 + e >= 0 && c0 + e < FW) {
-                                            wfoot[r * FS + c0 + e] = v[u][e];
-                                            if (DW) wfoot2[r * FS + c0 + e] = v2[DW ? u : 0][e];
-                                        }
+                                for (int e = 0; e < 4; e++) v[u][e] = 0.0f;
+                                if (t < nq) {
+                                    const int r = t / NQ, qq = t - r * NQ;
+                                    const int lin0 = (fj0 + r) * M + base + 4 * qq;
+                                    if (lin0 >= 0 && lin0 + 3 < MM) {
+                                        ld_quad(img_ptr + lin0, v[u]);
+                                    } else {
+#pragma unroll
+                                        for (int e = 0; e < 4; e++)
+                                            if (lin0 + e >= 0 && lin0 + e < MM) v[u][e] = ld_f32(img_ptr + lin0 + e);
+                                    }
+                                }
+                            }
+#pragma unroll
+                            for (int u = 0; u < KQ; u++) {
+                                const int t = lane + 32 * u;
+                                if (t < nq) {
+                                    const int r = t / NQ, qq = t - r * NQ;
+                                    const int c0 = 4 * qq - sh; // footprint column of the quad's first pixel
+                                    if (QALIGN) {
+                                        *reinterpret_cast<float4 *>(wfoot + r * FS + 4 * qq) =
+                                            make_float4(v[u][0], v[u][1], v[u][2], v[u][3]);
+                                    } else {
+#pragma unroll
+                                        for (int e = 0; e < 4; e++)
+                                            if (c0 + e >= 0 && c0 + e < FW) wfoot[r * FS + c0 + e] = v[u][e];
+                                    }
                                 }
                             }
                         }
