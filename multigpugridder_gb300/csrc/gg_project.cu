@@ -1318,13 +1318,52 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                         }
                     } else if (foot) {
                         // the forward projection's pixels: inside the image and the mask
-                        for (int t = lane; t < fh * FW; t += 32) {
-                            const int r = t / FW, c = t - r * FW;
-                            const int pi = fi0 + c, pj = fj0 + r, di = pi - imgCenter, dj = pj - imgCenter;
-                            float v = 0.0f;
-                            if (pi >= 0 && pi < M && pj >= 0 && pj < M && (long long)di * di + (long long)dj * dj <= R2)
-                                v = ld_f32(img_ptr + (size_t)pj * M + pi);
-                            wfoot[r * FS + c] = v;
+                        if (vecImg && !ONES) {
+                            // aligned pixel quads (4 divides M: a quad lies wholly inside or
+                            // outside the image rows), three in flight per lane at a time;
+                            // the mask is applied pixel by pixel
+                            constexpr int NQ = FW / 4 + 1; // quads per footprint row
+                            const int base = fi0 & ~3, sh = fi0 & 3, nq = fh * NQ;
+                            for (int t0 = lane; t0 < nq; t0 += 96) {
+                                float v[3][4];
+#pragma unroll
+                                for (int u = 0; u < 3; u++) {
+                                    const int t = t0 + 32 * u;
+#pragma unroll
+                                    for (int e = 0; e < 4; e++) v[u][e] = 0.0f;
+                                    const int r = t / NQ, qq = t - r * NQ;
+                                    const int pj = fj0 + r, pi = base + 4 * qq;
+                                    if (t < nq && pj >= 0 && pj < M && pi >= 0 && pi < M) {
+                                        ld_quad(img_ptr + (size_t)pj * M + pi, v[u]);
+                                        const long long dj = pj - imgCenter;
+#pragma unroll
+                                        for (int e = 0; e < 4; e++) {
+                                            const long long di = pi + e - imgCenter;
+                                            if (di * di + dj * dj > R2) v[u][e] = 0.0f;
+                                        }
+                                    }
+                                }
+#pragma unroll
+                                for (int u = 0; u < 3; u++) {
+                                    const int t = t0 + 32 * u;
+                                    if (t < nq) {
+                                        const int r = t / NQ, qq = t - r * NQ;
+                                        const int c0 = 4 * qq - sh; // footprint column of the quad's first pixel
+#pragma unroll
+                                        for (int e = 0; e < 4; e++)
+                                            if (c0 + e >= 0 && c0 + e < FW) wfoot[r * FS + c0 + e] = v[u][e];
+                                    }
+                                }
+                            }
+                        } else {
+                            for (int t = lane; t < fh * FW; t += 32) {
+                                const int r = t / FW, c = t - r * FW;
+                                const int pi = fi0 + c, pj = fj0 + r, di = pi - imgCenter, dj = pj - imgCenter;
+                                float v = 0.0f;
+                                if (pi >= 0 && pi < M && pj >= 0 && pj < M && (long long)di * di + (long long)dj * dj <= R2)
+                                    v = ld_f32(img_ptr + (size_t)pj * M + pi);
+                                wfoot[r * FS + c] = v;
+                            }
                         }
                     }
                 }
