@@ -5,7 +5,9 @@ plain gridder calls (gg_forward_project, gg_back_project + gg_get_cas_volume)
 within relative L2 1e-6 (cuFFT may pick other kernels for other batch
 sizes).  Admission by footprint: a request larger than the HBM budget fails
 with GG_ERR_OUT_OF_MEMORY, and a budget that fits one request at a time runs
-them one at a time."""
+them one at a time.  Chunked scheduling: requests split into chunks that
+interleave across lanes give the same results; short requests overtake a long
+one between its chunks; a backlog bound refuses submissions with GG_ERR_BUSY."""
 import ctypes
 
 import numpy as np
