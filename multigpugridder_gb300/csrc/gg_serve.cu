@@ -485,6 +485,7 @@ void worker_main(gg_server *S)
             if (admit) {
                 S->queued[r->high].erase(r);
                 S->queued_work -= r->est;
+                if (S->queued[0].empty() && S->queued[1].empty()) S->queued_work = 0; // no rounding drift
                 r->admitted = true;
                 S->used += r->footprint;
                 S->active++;
