@@ -381,12 +381,15 @@ def run_gb300(args):
     serve = prec = grad = ctf = None
     if rank == 0 and world == 1 and args.serve_seconds > 0:
         serve = run_serve(args)
+    prec128 = None
     if rank == 0 and world == 1 and not args.no_precision and args.size == 128:
-        prec, keep = run_precision(args)
+        prec, keep = run_precision(args, "256")
+        prec128, keep128 = run_precision(args, "128")
         if not args.no_cpu_baseline:
             # CPU leg: the FP64 oracle as the checker of the reduced-precision results
-            prec["vs_f64"] = check_precision_vs_f64(keep)
-        del keep
+            prec["vs_f64"] = check_precision_vs_f64(keep, "256")
+            prec128["vs_f64"] = check_precision_vs_f64(keep128, "128")
+        del keep, keep128
     if rank == 0 and world == 1 and not args.no_autograd and args.size == 128:
         grad = run_autograd(args)
     if rank == 0 and world == 1 and not args.no_ctf:
@@ -398,7 +401,8 @@ def run_gb300(args):
                "data": "synthetic (seeded Gaussian-blob volume, 100x100 direction grid)",
                "config": bench_config(args, world),
                "roofline": roofline, "cpu_baseline": base, "e2e": e2e, "gpu_launches": launches,
-               "clocks": clk, "step_ms": ms_steps, "serve": serve, "precision": prec, "autograd": grad,
+               "clocks": clk, "step_ms": ms_steps, "serve": serve, "precision": prec, "precision_128": prec128,
+               "autograd": grad,
                "ctf": ctf}
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -587,20 +591,35 @@ def run_serve(args):
 PREC_SUBSET = 64  # directions of the 5,000 compared against the FP64 oracle
 
 
-def precision_workload():
+PREC_WORKLOADS = {
+    "256": "256^3 volume (400 blobs), interpFactor 2 (CAS volume 518^3), 5,000 random-quaternion directions",
+    "128": "128^3 volume (100 blobs), interpFactor 2 (CAS volume 262^3), the 10,000 directions of the 100x100 grid",
+}
+
+
+def precision_workload(kind="256"):
+    """(N, directions, volume, axes, subset, batch, timed steps) of a precision
+    workload: "256" the 256^3 storage-precision configuration, "128" the
+    benchmark's own 128^3 step."""
     from multigpugridder_gb300 import synthetic
 
-    N, n = 256, 5000
-    vol = synthetic.blob_volume(N, 400, seed=3)
-    axes = synthetic.quaternion_axes(n, seed=3).astype(np.float32)
+    if kind == "128":
+        N, n = 128, 10000
+        vol = synthetic.blob_volume(N, 100, seed=2)
+        axes = synthetic.grid_axes(100, 100).astype(np.float32)
+        batch, reps = 2000, 3
+    else:
+        N, n = 256, 5000
+        vol = synthetic.blob_volume(N, 400, seed=3)
+        axes = synthetic.quaternion_axes(n, seed=3).astype(np.float32)
+        batch, reps = 1000, 1
     sub = np.linspace(0, n - 1, PREC_SUBSET).round().astype(int)
-    return N, n, vol, axes, sub
+    return N, n, vol, axes, sub, batch, reps
 
 
-def run_precision(args):
-    """256^3 Gaussian-blob volume (400 blobs), interpFactor 2 (CAS volume 518^3),
-    5,000 random-quaternion directions: setVolume + forwardProject +
-    reconstructVol with FP32, BF16 and FP16 storage (FP32 accumulation).
+def run_precision(args, kind="256"):
+    """setVolume + forwardProject + reconstructVol of a precision workload
+    (precision_workload) with FP32, BF16 and FP16 storage (FP32 accumulation).
     Reports pairs/s per storage type and the relative L2 of the images and the
     reconstruction against the FP32 path.  It also keeps, per storage type,
     the images of a fixed subset of 64 directions and a reconstructVol of the
@@ -612,7 +631,7 @@ def run_precision(args):
     from multigpugridder_gb300._lib import check, lib
 
     L = lib()
-    N, n, vol, axes, sub = precision_workload()
+    N, n, vol, axes, sub, batch, reps = precision_workload(kind)
     dev = torch.device("cuda", torch.cuda.current_device())
     d_vol = torch.from_numpy(np.ascontiguousarray(vol)).to(dev)
     d_axes = torch.from_numpy(np.ascontiguousarray(axes)).to(dev)
@@ -628,7 +647,7 @@ def run_precision(args):
 
     # "bf16_vol": BF16 volume, FP32 CAS images for the back projection
     for prec in ("f32", "bf16", "f16", "bf16_vol"):
-        g = gg.MultiGPUGridder(N, n, 2.0, MaxAxesToAllocate=1000, precision="bf16" if prec == "bf16_vol" else prec)
+        g = gg.MultiGPUGridder(N, n, 2.0, MaxAxesToAllocate=batch, precision="bf16" if prec == "bf16_vol" else prec)
         if prec == "bf16_vol":
             g.set_image_precision("f32")
         h = g.handle
@@ -644,10 +663,11 @@ def run_precision(args):
             step()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            step()
+            for _ in range(reps):
+                step()
             b.record(stream)
         torch.cuda.synchronize()
-        ms = a.elapsed_time(b)
+        ms = a.elapsed_time(b) / reps
         res = {"pairs_per_s": n / (ms / 1e3), "ms_per_step": ms}
         if prec == "f32":
             ref = {"images": imgs.clone(), "rec": rec.clone()}
@@ -666,20 +686,19 @@ def run_precision(args):
         g.close()
         del imgs, rec, rec_sub
     keep["input_images"] = sub_imgs_f32.cpu().numpy()
-    return {"workload": "256^3 volume (400 blobs), interpFactor 2 (CAS volume 518^3), 5,000 random-quaternion "
-                        "directions: setVolume + forwardProject + reconstructVol, storage f32/bf16/f16 (volume and "
-                        "CAS images) and bf16_vol (BF16 volume, FP32 CAS images), FP32 accumulation",
+    return {"workload": PREC_WORKLOADS[kind] + ": setVolume + forwardProject + reconstructVol, storage f32/bf16/f16 "
+                        "(volume and CAS images) and bf16_vol (BF16 volume, FP32 CAS images), FP32 accumulation",
             "results": out}, keep
 
 
-def check_precision_vs_f64(keep):
+def check_precision_vs_f64(keep, kind="256"):
     """FP64 oracle references for the precision leg (part of the CPU leg):
     forwardProject of the 64-direction subset and reconstructVol of the FP32
     path's images of those directions, both in FP64 on the host; returns
     rel-L2 of each storage type's images and reconstruction against them."""
     from oracle import oracle as O
 
-    N, n, vol, axes, sub = precision_workload()
+    N, n, vol, axes, sub, _, _ = precision_workload(kind)
     p = O.Params(N)
     t0 = time.perf_counter()
     ref_imgs, _ = O.forward_project(vol, axes[sub], p, precision="f64")
