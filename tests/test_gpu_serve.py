@@ -202,3 +202,30 @@ def test_backlog_bound_sheds_load(cuda):
         srv.set_max_backlog(0)
         out, _ = srv.wait(srv.submit(vid, "forward", axes[:5]))
         assert np.array_equal(out, outs[0][:5])
+
+
+def test_default_quantum_chunks_equal_plain_path(cuda, gglib):
+    """A 64^3 volume (CAS images of 128^2) with the default quantum: a
+    1,500-direction back request runs as chunks of 1,024 and 476 directions,
+    a forward request as chunks too, beside short requests; both equal the
+    plain gridder calls within relative L2 1e-6 and the same requests alone
+    bit for bit."""
+    from multigpugridder_gb300.serve import Server
+
+    N = 64
+    v = O.blob_volume(N, 20, seed=91).astype(np.float32)
+    axes = O.quaternion_axes(1500, 92).astype(np.float32)
+    imgs = np.random.default_rng(93).standard_normal((len(axes), N, N)).astype(np.float32)
+    with Server(lanes=4) as srv:
+        vid = srv.add_volume(v)
+        hb = srv.submit(vid, "back", axes, imgs)
+        hf = srv.submit(vid, "forward", axes)
+        hs = [srv.submit(vid, "forward", axes[k * 16:(k + 1) * 16]) for k in range(8)]
+        back = srv.wait(hb)[0].copy()
+        fwd = srv.wait(hf)[0].copy()
+        for h in hs:
+            srv.wait(h)
+        back_alone = srv.wait(srv.submit(vid, "back", axes, imgs))[0].copy()
+    assert np.array_equal(back, back_alone)
+    assert O.rel_l2(back, _plain(gglib, v, "back", axes, imgs)) < 1e-6
+    assert O.rel_l2(fwd, _plain(gglib, v, "forward", axes, None)) < 1e-6
