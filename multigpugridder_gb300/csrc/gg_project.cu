@@ -523,6 +523,10 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
 constexpr int kCBX = 16, kCBY = 8; // brick: 2x2x2 warp blocks of 8x4xBD (BD = 6, or 8 on large images)
 constexpr int kCThreads = 256;  // threads of a group
 constexpr int kBpGroups = 3;    // groups (bricks) per CTA, one CTA per SM
+// The adjoint's 6-deep form runs two groups per CTA: with its 24-wide footprints the
+// voxel queue's two buffers fit only beside two groups (adjoint of 4,096 directions at
+// 128^3: 67.8 ms with three one-buffer groups, 62.0 ms with two queued ones).
+template <bool ADJ, bool DEEP> constexpr int kGroupsOf = (ADJ && !DEEP) ? 2 : kBpGroups;
 static_assert(kBpChunk % kCThreads == 0, "the cull gives each thread kBpChunk / kCThreads directions");
 // Depth of a warp block: 6 voxels, or 8 (DEEP, reference rule) on CAS images
 // of 512^2 and more.  Deeper blocks have more active voxels per direction
@@ -810,13 +814,14 @@ struct alignas(16) BpDirMeta {
 // A warp's queue of voxel windows: entries (block voxel | footprint buffer
 // << 8) in direction order, run 32 at a time, so that rounds are full across
 // directions.  NB footprint buffers per warp: 2 where shared memory allows
-// (a direction's footprint is staged while the previous direction's last
+// (the 6-deep reference-rule form, and the adjoint's with two groups per CTA;
+// a direction's footprint is staged while the previous direction's last
 // voxels still wait in the queue); else 1, and each direction's active voxels
 // run at once from the same array (a plain list, no queue): queue rounds with
 // one buffer measured slower (per-lane direction records, spills).
 template <bool ADJ, bool DW, bool DEEP>
 struct BpQueue {
-    static constexpr int NB = (!ADJ && !DW && !DEEP) ? 2 : 1;
+    static constexpr int NB = (!DW && !DEEP) ? 2 : 1;
     static constexpr int NEED = (NB - 1) * 31 + BpShape<ADJ, DW, DEEP>::WV; // most entries held at once
     static constexpr int CAP = NEED <= 128 ? 128 : (NEED <= 256 ? 256 : 512);
 };
@@ -1349,9 +1354,14 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                     if (t < nq) {
                                         const int r = t / NQ, qq = t - r * NQ;
                                         const int c0 = 4 * qq - sh; // footprint column of the quad's first pixel
+                                        if (QALIGN) {
+                                            *reinterpret_cast<float4 *>(wfoot + r * FS + 4 * qq) =
+                                                make_float4(v[u][0], v[u][1], v[u][2], v[u][3]);
+                                        } else {
 #pragma unroll
-                                        for (int e = 0; e < 4; e++)
-                                            if (c0 + e >= 0 && c0 + e < FW) wfoot[r * FS + c0 + e] = v[u][e];
+                                            for (int e = 0; e < 4; e++)
+                                                if (c0 + e >= 0 && c0 + e < FW) wfoot[r * FS + c0 + e] = v[u][e];
+                                        }
                                     }
                                 }
                             }
@@ -1362,7 +1372,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                 float v = 0.0f;
                                 if (pi >= 0 && pi < M && pj >= 0 && pj < M && (long long)di * di + (long long)dj * dj <= R2)
                                     v = ld_f32(img_ptr + (size_t)pj * M + pi);
-                                wfoot[r * FS + c] = v;
+                                wfoot[r * FS + c + (QALIGN ? (fi0 & 3) : 0)] = v;
                             }
                         }
                     }
@@ -1480,7 +1490,7 @@ static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *k
             return launch_bp_compact_g<TI, ONES, DENS, ADJ, DW, DEEP, 1>(vol, img, ker, axes, n, g, scale, s, pd,
                                                                          zero_edges, img2, 1);
     }
-    return launch_bp_compact_g<TI, ONES, DENS, ADJ, DW, DEEP, kBpGroups>(vol, img, ker, axes, n, g, scale, s, pd,
+    return launch_bp_compact_g<TI, ONES, DENS, ADJ, DW, DEEP, kGroupsOf<ADJ, DEEP>>(vol, img, ker, axes, n, g, scale, s, pd,
                                                                          zero_edges, img2, 32);
 }
 
