@@ -523,10 +523,11 @@ __device__ __forceinline__ void ref_window(const RefWindow &q, const float *sker
 constexpr int kCBX = 16, kCBY = 8; // brick: 2x2x2 warp blocks of 8x4xBD (BD = 6, or 8 on large images)
 constexpr int kCThreads = 256;  // threads of a group
 constexpr int kBpGroups = 3;    // groups (bricks) per CTA, one CTA per SM
-// The adjoint's 6-deep form runs two groups per CTA: with its 24-wide footprints the
-// voxel queue's two buffers fit only beside two groups (adjoint of 4,096 directions at
-// 128^3: 67.8 ms with three one-buffer groups, 62.0 ms with two queued ones).
-template <bool ADJ, bool DEEP> constexpr int kGroupsOf = (ADJ && !DEEP) ? 2 : kBpGroups;
+// The adjoint's and the two-stack form's 6-deep kernels run two groups per CTA: with the
+// adjoint's 24-wide footprints, or the second stack's footprints, the voxel queue's two
+// buffers fit only beside two groups (adjoint of 4,096 directions at 128^3: 67.8 ms with
+// three one-buffer groups, 62.0 ms with two queued ones).
+template <bool ADJ, bool DW, bool DEEP> constexpr int kGroupsOf = ((ADJ || DW) && !DEEP) ? 2 : kBpGroups;
 static_assert(kBpChunk % kCThreads == 0, "the cull gives each thread kBpChunk / kCThreads directions");
 // Depth of a warp block: 6 voxels, or 8 (DEEP, reference rule) on CAS images
 // of 512^2 and more.  Deeper blocks have more active voxels per direction
@@ -821,7 +822,7 @@ struct alignas(16) BpDirMeta {
 // one buffer measured slower (per-lane direction records, spills).
 template <bool ADJ, bool DW, bool DEEP>
 struct BpQueue {
-    static constexpr int NB = (!DW && !DEEP) ? 2 : 1;
+    static constexpr int NB = !DEEP ? 2 : 1;
     static constexpr int NEED = (NB - 1) * 31 + BpShape<ADJ, DW, DEEP>::WV; // most entries held at once
     static constexpr int CAP = NEED <= 128 ? 128 : (NEED <= 256 ? 256 : 512);
 };
@@ -1040,7 +1041,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                 const float *fb = wfoot + rj * FS + ri + (QALIGN ? (fi0 & 3) : 0);
                 const float pi0 = (float)(imgi - HALF - imgCenter), pj0 = (float)(imgj - HALF - imgCenter);
                 foot_window_x2<DENS, W, W, FS, DW, TS>(fwin, fb, tab, pi0, pj0, cs, cw,
-                                                DW ? wfoot2 + rj * FS + ri : nullptr);
+                                                DW ? wfoot2 + rj * FS + ri + (QALIGN ? (fi0 & 3) : 0) : nullptr);
             } else if (ADJ) {
                 cs = adjoint_window_slow<TI>(vi, vj, vk, volCenter, nx0, nx1, nx2, ny0, ny1, ny2, img_ptr, M,
                                              imgCenter, maskR, sker, cp, kerScale, kerCenterHalf, kerSize);
@@ -1240,12 +1241,18 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                             v2[e] = __ldg(img2_ptr + lin0 + e);
                                         }
                                 }
+                                if (QALIGN) {
+                                    *reinterpret_cast<float4 *>(wfoot + r * FS + 4 * qq) = make_float4(v[0], v[1], v[2], v[3]);
+                                    *reinterpret_cast<float4 *>(wfoot2 + r * FS + 4 * qq) =
+                                        make_float4(v2[0], v2[1], v2[2], v2[3]);
+                                } else {
 #pragma unroll
-                                for (int e = 0; e < 4; e++)
-                                    if (c0 + e >= 0 && c0 + e < FW) {
-                                        wfoot[r * FS + c0 + e] = v[e];
-                                        wfoot2[r * FS + c0 + e] = v2[e];
-                                    }
+                                    for (int e = 0; e < 4; e++)
+                                        if (c0 + e >= 0 && c0 + e < FW) {
+                                            wfoot[r * FS + c0 + e] = v[e];
+                                            wfoot2[r * FS + c0 + e] = v2[e];
+                                        }
+                                }
                             }
                         } else {
                             // a lane's quads (at most KQ) are all loaded before any is
@@ -1319,7 +1326,7 @@ bp_ref_compact_kernel(float *__restrict__ vol, float *__restrict__ pd, int V, co
                                 if (DW) v2 = __ldg(img2_ptr + lin);
                             }
                             wfoot[r * FS + c + (QALIGN ? (fi0 & 3) : 0)] = v;
-                            if (DW) wfoot2[r * FS + c] = v2;
+                            if (DW) wfoot2[r * FS + c + (QALIGN ? (fi0 & 3) : 0)] = v2;
                         }
                     } else if (foot) {
                         // the forward projection's pixels: inside the image and the mask
@@ -1490,7 +1497,7 @@ static cudaError_t launch_bp_compact_t(float *vol, const TI *img, const float *k
             return launch_bp_compact_g<TI, ONES, DENS, ADJ, DW, DEEP, 1>(vol, img, ker, axes, n, g, scale, s, pd,
                                                                          zero_edges, img2, 1);
     }
-    return launch_bp_compact_g<TI, ONES, DENS, ADJ, DW, DEEP, kGroupsOf<ADJ, DEEP>>(vol, img, ker, axes, n, g, scale, s, pd,
+    return launch_bp_compact_g<TI, ONES, DENS, ADJ, DW, DEEP, kGroupsOf<ADJ, DW, DEEP>>(vol, img, ker, axes, n, g, scale, s, pd,
                                                                          zero_edges, img2, 32);
 }
 
